@@ -1,0 +1,571 @@
+// C ABI of the propagator: host logic of cudaprob3::Propagator<FLOAT_T>
+// (propagator.hpp:43-337) and cudaprob3::CudaPropagatorSingle<FLOAT_T>
+// (cudapropagator.cuh:39-251), restated with per-handle state and status codes.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <string>
+#include <vector>
+
+#include "../../include/cudaprob3_gb300.h"
+#include "cp3_launch.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+    return fail(CP3_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+// Makes `dev` current for the scope and restores the caller's device.
+struct DeviceGuard {
+    int prev = -1;
+    cudaError_t err = cudaSuccess;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) err = cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t ensure(size_t count) {
+        if (count <= n && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+        if (e == cudaSuccess) n = count;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+}  // namespace
+
+struct cp3_propagator {
+    int device = 0;
+    int n_cos = 0, n_en = 0;
+    bool mixed = false;
+
+    // host state of Propagator (propagator.hpp:317-336)
+    std::vector<double> energies, cosines;
+    std::vector<int> maxlayers;
+    std::vector<double> radii, rhos, ye, coslimit;  // descending radii after setDensity
+    double th12 = 0, th13 = 0, th23 = 0, dcp = 0, dm12 = 0, dm23 = 0;
+    double height_cm = 0;
+    bool has_mns = false, has_masses = false, has_density = false;
+    bool has_energy = false;
+    bool is_set_cosine = false, is_set_height = false;
+
+    // device state
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    DevBuf<double> d_energy, d_cosine, d_radii, d_rhoye;
+    DevBuf<int> d_maxl;
+    DevBuf<unsigned char> d_tab, d_pe, d_len, d_result;
+    DevBuf<int2> d_ptab;
+    void* ext_result = nullptr;
+    size_t ext_bytes = 0;
+    bool maxl_dirty = true, energy_dirty = true, cosine_dirty = true, density_dirty = true;
+
+    // pinned host copy for getProbability (cudapropagator.cuh:73, 168-181)
+    void* h_result = nullptr;
+    bool results_on_host = false;
+    int last_launches = 0;
+
+    // launch shape
+    int te = 64, groups = 4, cchunk = 32;
+
+    size_t elem() const { return mixed ? sizeof(float) : sizeof(double); }
+    size_t result_bytes() const { return (size_t)9 * n_cos * n_en * elem(); }
+    void* result_ptr() const { return ext_result ? ext_result : (void*)d_result.p; }
+};
+
+namespace {
+
+// propagator.hpp:301-307: layers crossed = number of cosine limits above c.
+void set_maxlayers(cp3_propagator* p) {
+    for (int ic = 0; ic < p->n_cos; ic++) {
+        const double c = p->cosines[ic];
+        int cnt = 0;
+        for (double lim : p->coslimit) cnt += (c < lim);
+        p->maxlayers[ic] = cnt;
+    }
+    p->maxl_dirty = true;
+}
+
+int check(cp3_propagator* p) {
+    if (!p) return fail(CP3_ERR_ARGUMENT, "null propagator handle");
+    return CP3_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cp3_abi_version(void) { return CP3_ABI_VERSION; }
+
+const char* cp3_last_error(void) { return g_last_error.c_str(); }
+
+int cp3_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+int cp3_create(cp3_propagator** out, int device_id, int n_cosines, int n_energies, int precision) {
+    if (!out) return fail(CP3_ERR_ARGUMENT, "cp3_create: null output pointer");
+    *out = nullptr;
+    if (n_cosines < 0 || n_energies < 0) return fail(CP3_ERR_ARGUMENT, "cp3_create: negative grid size");
+    if (precision != CP3_PRECISION_FP64 && precision != CP3_PRECISION_MIXED)
+        return fail(CP3_ERR_ARGUMENT, "cp3_create: unknown precision");
+    int n_dev = 0;
+    cudaError_t e = cudaGetDeviceCount(&n_dev);
+    if (e != cudaSuccess || n_dev == 0) {
+        cudaGetLastError();
+        return fail(CP3_ERR_NO_DEVICE, "No GPU found");
+    }
+    if (device_id < 0 || device_id >= n_dev)
+        return fail(CP3_ERR_NO_DEVICE,
+                    "The requested GPU Id " + std::to_string(device_id) + " is not available.");
+    DeviceGuard g(device_id);
+    if (g.err != cudaSuccess) return cuda_fail(g.err, "cudaSetDevice");
+    cp3_propagator* p = new cp3_propagator();
+    p->device = device_id;
+    p->n_cos = n_cosines;
+    p->n_en = n_energies;
+    p->mixed = (precision == CP3_PRECISION_MIXED);
+    p->energies.assign(n_energies, 0.0);
+    p->cosines.assign(n_cosines, 0.0);
+    p->maxlayers.assign(n_cosines, 0);
+    if (!p->mixed) {
+        p->te = 64;
+        p->groups = 2;
+        p->cchunk = 32;
+    }
+    auto bail = [&](cudaError_t err, const char* where) {
+        int rc = cuda_fail(err, where);
+        cp3_destroy(p);
+        return rc;
+    };
+    if ((e = cudaStreamCreateWithFlags(&p->own_stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return bail(e, "cudaStreamCreate");
+    p->stream = p->own_stream;
+    if ((e = p->d_energy.ensure(std::max(n_energies, 1))) != cudaSuccess) return bail(e, "cudaMalloc");
+    if ((e = p->d_cosine.ensure(std::max(n_cosines, 1))) != cudaSuccess) return bail(e, "cudaMalloc");
+    if ((e = p->d_maxl.ensure(std::max(n_cosines, 1))) != cudaSuccess) return bail(e, "cudaMalloc");
+    if ((e = p->d_result.ensure(std::max<size_t>(p->result_bytes(), 16))) != cudaSuccess)
+        return bail(e, "cudaMalloc");
+    if (p->mixed) {
+        // Q1.30 cos/sin of 2*pi*j/256, j = -128..128
+        std::vector<int2> tab(cp3::kPhaseTabN + 1);
+        for (int j = -cp3::kPhaseTabN / 2; j <= cp3::kPhaseTabN / 2; j++) {
+            const double ang = cp3::kTwoPi * j / cp3::kPhaseTabN;
+            tab[j + cp3::kPhaseTabN / 2] = make_int2((int)std::llround(std::cos(ang) * 1073741824.0),
+                                                      (int)std::llround(std::sin(ang) * 1073741824.0));
+        }
+        if ((e = p->d_ptab.ensure(tab.size())) != cudaSuccess) return bail(e, "cudaMalloc");
+        if ((e = cudaMemcpy(p->d_ptab.p, tab.data(), tab.size() * sizeof(int2), cudaMemcpyHostToDevice)) !=
+            cudaSuccess)
+            return bail(e, "cudaMemcpy");
+    }
+    *out = p;
+    return CP3_OK;
+}
+
+int cp3_destroy(cp3_propagator* p) {
+    if (!p) return CP3_OK;
+    DeviceGuard g(p->device);
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    p->d_energy.release();
+    p->d_cosine.release();
+    p->d_radii.release();
+    p->d_rhoye.release();
+    p->d_maxl.release();
+    p->d_tab.release();
+    p->d_pe.release();
+    p->d_len.release();
+    p->d_result.release();
+    p->d_ptab.release();
+    if (p->h_result) cudaFreeHost(p->h_result);
+    if (p->own_stream) cudaStreamDestroy(p->own_stream);
+    delete p;
+    return CP3_OK;
+}
+
+int cp3_set_energy_list(cp3_propagator* p, const double* list, int n) {
+    if (int rc = check(p)) return rc;
+    if (n != p->n_en)
+        return fail(CP3_ERR_ARGUMENT,
+                    "Propagator::setEnergyList. Propagator was not created for this number of energy nodes");
+    if (n > 0 && !list) return fail(CP3_ERR_ARGUMENT, "setEnergyList: null list");
+    for (int i = 0; i < n; i++)
+        if (!(list[i] > 0.0) || !std::isfinite(list[i]))
+            return fail(CP3_ERR_ARGUMENT, "setEnergyList: energies must be finite and positive");
+    p->energies.assign(list, list + n);
+    p->has_energy = true;
+    p->energy_dirty = true;
+    return CP3_OK;
+}
+
+int cp3_set_production_height(cp3_propagator* p, double height_km) {
+    if (int rc = check(p)) return rc;
+    if (!p->is_set_cosine) return fail(CP3_ERR_STATE, "must set cosine list before production height");
+    if (!std::isfinite(height_km)) return fail(CP3_ERR_ARGUMENT, "setProductionHeight: height must be finite");
+    p->height_cm = height_km * 100000.0;
+    p->is_set_height = true;
+    return CP3_OK;
+}
+
+int cp3_set_cosine_list(cp3_propagator* p, const double* list, int n) {
+    if (int rc = check(p)) return rc;
+    if (n != p->n_cos)
+        return fail(CP3_ERR_ARGUMENT,
+                    "Propagator::setCosineList. Propagator was not created for this number of cosine nodes");
+    if (n > 0 && !list) return fail(CP3_ERR_ARGUMENT, "setCosineList: null list");
+    for (int i = 0; i < n; i++)
+        if (!(list[i] >= -1.0 && list[i] <= 1.0))
+            return fail(CP3_ERR_ARGUMENT, "setCosineList: cosines must lie in [-1, 1]");
+    p->cosines.assign(list, list + n);
+    if (p->is_set_height) p->height_cm = (p->height_cm / 100000.0) * 100000.0;
+    set_maxlayers(p);
+    p->is_set_cosine = true;
+    p->cosine_dirty = true;
+    return CP3_OK;
+}
+
+int cp3_set_mns_matrix(cp3_propagator* p, double t12, double t13, double t23, double dcp) {
+    if (int rc = check(p)) return rc;
+    if (!std::isfinite(t12) || !std::isfinite(t13) || !std::isfinite(t23) || !std::isfinite(dcp))
+        return fail(CP3_ERR_ARGUMENT, "setMNSMatrix: angles must be finite");
+    p->th12 = t12;
+    p->th13 = t13;
+    p->th23 = t23;
+    p->dcp = dcp;
+    p->has_mns = true;
+    return CP3_OK;
+}
+
+int cp3_set_neutrino_masses(cp3_propagator* p, double dm12sq, double dm23sq) {
+    if (int rc = check(p)) return rc;
+    if (!std::isfinite(dm12sq) || !std::isfinite(dm23sq))
+        return fail(CP3_ERR_ARGUMENT, "setNeutrinoMasses: mass splittings must be finite");
+    p->dm12 = dm12sq;
+    p->dm23 = dm23sq;
+    p->has_masses = true;
+    return CP3_OK;
+}
+
+int cp3_set_density(cp3_propagator* p, const double* radii, const double* rhos, const double* ye, int n) {
+    if (int rc = check(p)) return rc;
+    if (n <= 0) return fail(CP3_ERR_ARGUMENT, "setDensity : vectors must not be empty");
+    if (!radii || !rhos) return fail(CP3_ERR_ARGUMENT, "setDensity : null array");
+    if (n > CP3_MAX_ROWS)
+        return fail(CP3_ERR_LIMIT, "setDensity : more than " + std::to_string(CP3_MAX_ROWS) + " rows");
+    for (int i = 0; i < n; i++) {
+        if (!std::isfinite(radii[i]) || !std::isfinite(rhos[i]) || radii[i] < 0.0 || rhos[i] < 0.0)
+            return fail(CP3_ERR_ARGUMENT, "setDensity : radii and densities must be finite and >= 0");
+        if (ye && !(ye[i] >= 0.0 && ye[i] <= 1.0))
+            return fail(CP3_ERR_ARGUMENT, "setDensity : electron fractions must lie in [0, 1]");
+    }
+    // propagator.hpp:127-147: one monotone order, flipped to outside-in
+    bool flip = false;
+    if (n >= 2) {
+        const int sign = (radii[1] - radii[0] > 0 ? 1 : -1);
+        for (int i = 1; i < n; i++)
+            if ((radii[i] - radii[i - 1]) * sign < 0) return fail(CP3_ERR_ARGUMENT, "radii order messed up");
+        flip = (sign == 1);
+    }
+    p->radii.resize(n);
+    p->rhos.resize(n);
+    p->ye.resize(n);
+    for (int i = 0; i < n; i++) {
+        const int s = flip ? n - 1 - i : i;
+        p->radii[i] = radii[s];
+        p->rhos[i] = rhos[s];
+        p->ye[i] = ye ? ye[s] : 0.5;
+    }
+    // propagator.hpp:149-158
+    p->coslimit.resize(n);
+    for (int i = 0; i < n; i++) {
+        double x = -1 * std::sqrt(1 - (p->radii[i] * p->radii[i] / (cp3::kREarth * cp3::kREarth)));
+        if (i == 0) x = 0;
+        p->coslimit[i] = x;
+    }
+    set_maxlayers(p);
+    p->has_density = true;
+    p->density_dirty = true;
+    return CP3_OK;
+}
+
+int cp3_set_density_from_file(cp3_propagator* p, const char* path) {
+    if (int rc = check(p)) return rc;
+    if (!path) return fail(CP3_ERR_ARGUMENT, "setDensityFromFile: null path");
+    std::ifstream file(path);
+    if (!file) return fail(CP3_ERR_FILE, std::string("could not open density file ") + path);
+    std::vector<double> r, d;
+    double a, b;
+    while (file >> a >> b) {
+        r.push_back(a);
+        d.push_back(b);
+    }
+    return cp3_set_density(p, r.data(), d.data(), nullptr, (int)r.size());
+}
+
+int cp3_set_stream(cp3_propagator* p, void* s) {
+    if (int rc = check(p)) return rc;
+    p->stream = s ? (cudaStream_t)s : p->own_stream;
+    return CP3_OK;
+}
+
+int cp3_set_result_buffer(cp3_propagator* p, void* dptr, size_t bytes) {
+    if (int rc = check(p)) return rc;
+    if (dptr && bytes < p->result_bytes())
+        return fail(CP3_ERR_ARGUMENT, "set_result_buffer: buffer smaller than 9*n_cos*n_en elements");
+    p->ext_result = dptr;
+    p->ext_bytes = dptr ? bytes : 0;
+    p->results_on_host = false;
+    return CP3_OK;
+}
+
+int cp3_calculate_probabilities_async(cp3_propagator* p, int type) {
+    if (int rc = check(p)) return rc;
+    if (!p->is_set_height)
+        return fail(CP3_ERR_STATE, "CudaPropagatorSingle::calculateProbabilities. production height was not set");
+    if (!p->has_density) return fail(CP3_ERR_STATE, "CudaPropagatorSingle::calculateProbabilities. density was not set");
+    if (!p->has_mns || !p->has_masses)
+        return fail(CP3_ERR_STATE,
+                    "CudaPropagatorSingle::calculateProbabilities. mixing matrix or neutrino masses were not set");
+    if (p->n_en > 0 && !p->has_energy)
+        return fail(CP3_ERR_STATE, "CudaPropagatorSingle::calculateProbabilities. energy list was not set");
+    if (type != CP3_NEUTRINO && type != CP3_ANTINEUTRINO)
+        return fail(CP3_ERR_ARGUMENT, "calculateProbabilities: unknown neutrino type");
+    p->results_on_host = false;
+    p->last_launches = 0;
+    if (p->n_cos == 0 || p->n_en == 0) return CP3_OK;
+    DeviceGuard g(p->device);
+    if (g.err != cudaSuccess) return cuda_fail(g.err, "cudaSetDevice");
+    cudaError_t e;
+    const int n = (int)p->radii.size();
+    const int nl = n + 1;
+    const int nl_pad = (nl + 1) / 2 * 2;
+    // uploads of changed inputs (cudapropagator.cuh:132-159, 184-188)
+    if (p->energy_dirty) {
+        if ((e = cudaMemcpyAsync(p->d_energy.p, p->energies.data(), sizeof(double) * p->n_en,
+                                 cudaMemcpyHostToDevice, p->stream)) != cudaSuccess)
+            return cuda_fail(e, "cudaMemcpyAsync(energies)");
+        p->energy_dirty = false;
+    }
+    if (p->cosine_dirty) {
+        if ((e = cudaMemcpyAsync(p->d_cosine.p, p->cosines.data(), sizeof(double) * p->n_cos,
+                                 cudaMemcpyHostToDevice, p->stream)) != cudaSuccess)
+            return cuda_fail(e, "cudaMemcpyAsync(cosines)");
+        p->cosine_dirty = false;
+    }
+    if (p->maxl_dirty) {
+        if ((e = cudaMemcpyAsync(p->d_maxl.p, p->maxlayers.data(), sizeof(int) * p->n_cos, cudaMemcpyHostToDevice,
+                                 p->stream)) != cudaSuccess)
+            return cuda_fail(e, "cudaMemcpyAsync(maxlayers)");
+        p->maxl_dirty = false;
+    }
+    if (p->density_dirty) {
+        std::vector<double> rhoye(nl);
+        rhoye[0] = 0.0;
+        for (int i = 0; i < n; i++) rhoye[i + 1] = p->rhos[i] * p->ye[i];
+        if ((e = p->d_radii.ensure(n)) != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+        if ((e = p->d_rhoye.ensure(nl)) != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+        if ((e = cudaMemcpyAsync(p->d_radii.p, p->radii.data(), sizeof(double) * n, cudaMemcpyHostToDevice,
+                                 p->stream)) != cudaSuccess)
+            return cuda_fail(e, "cudaMemcpyAsync(radii)");
+        if ((e = cudaMemcpyAsync(p->d_rhoye.p, rhoye.data(), sizeof(double) * nl, cudaMemcpyHostToDevice,
+                                 p->stream)) != cudaSuccess)
+            return cuda_fail(e, "cudaMemcpyAsync(rhoye)");
+        // the staged copy must finish before `rhoye` leaves scope
+        if ((e = cudaStreamSynchronize(p->stream)) != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+        p->density_dirty = false;
+    }
+    // launch shape: the energy tile must leave room for the layer table
+    int te = p->te, groups = p->groups, cchunk = p->cchunk;
+    size_t smem = cp3::propagate_smem_bytes(p->mixed, te, nl, nl_pad, cchunk);
+    while (smem > 227 * 1024 && te > 32) {
+        te /= 2;
+        groups = std::min(groups * 2, 256 / te);
+        smem = cp3::propagate_smem_bytes(p->mixed, te, nl, nl_pad, cchunk);
+    }
+    while (smem > 227 * 1024 && cchunk > 8) {
+        cchunk /= 2;
+        smem = cp3::propagate_smem_bytes(p->mixed, te, nl, nl_pad, cchunk);
+    }
+    if (smem > 227 * 1024) return fail(CP3_ERR_LIMIT, "density table too large for one energy tile");
+    const int n_en_pad = (p->n_en + te - 1) / te * te;
+    const size_t word = p->mixed ? 4 : 8;
+    const size_t W = p->mixed ? cp3::kMixedWords : cp3::kFp64Words;
+    if ((e = p->d_tab.ensure((size_t)n_en_pad * nl * W * word)) != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    if ((e = p->d_pe.ensure((size_t)cp3::kPerEWords * n_en_pad * word)) != cudaSuccess)
+        return cuda_fail(e, "cudaMalloc");
+    if ((e = p->d_len.ensure((size_t)p->n_cos * nl_pad * 8)) != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+
+    cp3::PrepArgs pa{};
+    pa.pb.n_cos = p->n_cos;
+    pa.pb.n_en = p->n_en;
+    pa.pb.n_en_pad = n_en_pad;
+    pa.pb.te = te;
+    pa.pb.nl = nl;
+    pa.pb.nl_pad = nl_pad;
+    pa.pb.energies = p->d_energy.p;
+    pa.pb.cosines = p->d_cosine.p;
+    pa.pb.maxlayers = p->d_maxl.p;
+    pa.pb.radii = p->d_radii.p;
+    pa.pb.rhoye = p->d_rhoye.p;
+    pa.pb.height_cm = p->height_cm;
+    // propagator.hpp:226-248 (degeneracy break) and 191-221 (mixing matrix)
+    {
+        double mv[3] = {0.0, p->dm12, p->dm12 + p->dm23};
+        const double delta = 5.0e-9;
+        if (p->dm12 == 0.0) mv[0] -= delta;
+        if (p->dm23 == 0.0) mv[2] += delta;
+        cp3::OscParams& o = pa.osc;
+        o.dm01 = mv[0] - mv[1];
+        o.dm02 = mv[0] - mv[2];
+        o.d1 = -o.dm01;
+        o.d2 = -o.dm02;
+        const double s12 = std::sin(p->th12), c12 = std::cos(p->th12);
+        const double s13 = std::sin(p->th13), c13 = std::cos(p->th13);
+        o.u00 = (c12 * c13) * (c12 * c13);
+        o.u01 = (s12 * c13) * (s12 * c13);
+        o.u02 = s13 * s13;
+        const double O[9] = {c13 * c12, c13 * s12, s13, -s12, c12, 0.0, -s13 * c12, -s13 * s12, c13};
+        std::memcpy(o.o, O, sizeof O);
+        o.s23 = std::sin(p->th23);
+        o.c23 = std::cos(p->th23);
+        o.sd = std::sin(p->dcp);
+        o.cd = std::cos(p->dcp);
+        o.anti = (type == CP3_ANTINEUTRINO) ? 1 : 0;
+    }
+    pa.tab = p->d_tab.p;
+    pa.pe = p->d_pe.p;
+    pa.len = p->d_len.p;
+    if ((e = cp3::launch_prep(p->mixed, pa, p->stream)) != cudaSuccess) return cuda_fail(e, "prep kernel");
+
+    cp3::PropArgs ka{};
+    ka.tab = p->d_tab.p;
+    ka.pe = p->d_pe.p;
+    ka.len = p->d_len.p;
+    ka.maxl = p->d_maxl.p;
+    ka.ptab = p->d_ptab.p;
+    ka.out = p->result_ptr();
+    ka.n_cos = p->n_cos;
+    ka.n_en = p->n_en;
+    ka.n_en_pad = n_en_pad;
+    ka.nl = nl;
+    ka.nl_pad = nl_pad;
+    ka.cchunk = cchunk;
+    ka.c23 = pa.osc.c23;
+    ka.s23 = pa.osc.s23;
+    ka.cd = pa.osc.cd;
+    ka.sd = pa.osc.sd;
+    ka.q_c23 = (int)std::llround(ka.c23 * 1073741824.0);
+    ka.q_s23 = (int)std::llround(ka.s23 * 1073741824.0);
+    ka.q_cd = (int)std::llround(ka.cd * 1073741824.0);
+    ka.q_sd = (int)std::llround(ka.sd * 1073741824.0);
+    if ((e = cp3::launch_propagate(p->mixed, ka, te, groups, smem, p->stream)) != cudaSuccess)
+        return cuda_fail(e, "propagate kernel");
+    p->last_launches = 2;
+    return CP3_OK;
+}
+
+int cp3_wait_for_completion(cp3_propagator* p) {
+    if (int rc = check(p)) return rc;
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaStreamSynchronize(p->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+    return CP3_OK;
+}
+
+int cp3_calculate_probabilities(cp3_propagator* p, int type) {
+    int rc = cp3_calculate_probabilities_async(p, type);
+    if (rc != CP3_OK) return rc;
+    return cp3_wait_for_completion(p);
+}
+
+int cp3_result_bytes(cp3_propagator* p, size_t* bytes) {
+    if (int rc = check(p)) return rc;
+    if (!bytes) return fail(CP3_ERR_ARGUMENT, "null output pointer");
+    *bytes = p->result_bytes();
+    return CP3_OK;
+}
+
+int cp3_result_device_ptr(cp3_propagator* p, void** dptr) {
+    if (int rc = check(p)) return rc;
+    if (!dptr) return fail(CP3_ERR_ARGUMENT, "null output pointer");
+    *dptr = p->result_ptr();
+    return CP3_OK;
+}
+
+int cp3_copy_results_to_host(cp3_propagator* p, void* dst, size_t bytes) {
+    if (int rc = check(p)) return rc;
+    if (!dst || bytes < p->result_bytes()) return fail(CP3_ERR_ARGUMENT, "copy_results_to_host: destination too small");
+    if (p->result_bytes() == 0) return CP3_OK;
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaMemcpyAsync(dst, p->result_ptr(), p->result_bytes(), cudaMemcpyDeviceToHost, p->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(results)");
+    return CP3_OK;
+}
+
+int cp3_get_probability(cp3_propagator* p, int ic, int ie, int t, double* out) {
+    if (int rc = check(p)) return rc;
+    if (!out) return fail(CP3_ERR_ARGUMENT, "null output pointer");
+    if (ic >= p->n_cos || ie >= p->n_en || ic < 0 || ie < 0)
+        return fail(CP3_ERR_ARGUMENT, "CudaPropagatorSingle::getProbability. Invalid indices");
+    if (t < 0 || t > 8) return fail(CP3_ERR_ARGUMENT, "getProbability: ProbType out of range");
+    if (!p->results_on_host) {
+        DeviceGuard g(p->device);
+        if (!p->h_result) {
+            cudaError_t e = cudaMallocHost(&p->h_result, std::max<size_t>(p->result_bytes(), 16));
+            if (e != cudaSuccess) {
+                p->h_result = nullptr;
+                return cuda_fail(e, "cudaMallocHost");
+            }
+        }
+        int rc = cp3_copy_results_to_host(p, p->h_result, p->result_bytes());
+        if (rc != CP3_OK) return rc;
+        p->results_on_host = true;
+    }
+    const size_t idx = (size_t)t * p->n_en * p->n_cos + (size_t)ic * p->n_en + ie;
+    *out = p->mixed ? (double)((const float*)p->h_result)[idx] : ((const double*)p->h_result)[idx];
+    return CP3_OK;
+}
+
+int cp3_last_launch_count(cp3_propagator* p, int* launches) {
+    if (int rc = check(p)) return rc;
+    if (!launches) return fail(CP3_ERR_ARGUMENT, "null output pointer");
+    *launches = p->last_launches;
+    return CP3_OK;
+}
+
+}  // extern "C"

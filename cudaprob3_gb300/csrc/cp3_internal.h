@@ -1,0 +1,67 @@
+// Shared definitions of the GB300 Barger propagator (host and device).
+//
+// Physics constants are the reference's (constants.hpp:25-41, physics.hpp:442).
+// The per-layer amplitude follows Barger et al. (Phys. Rev. D 22, 2718):
+// eigenvalues of 2E*H from the trigonometric cubic (Eqs. 21-22, restated from
+// physics.hpp:268-341) and the propagator sum over eigenvalues (Eqs. 10-11,
+// physics.hpp:346-517), written here in an eigen-basis of a real matrix:
+//
+//   H_f = W H_r W^dagger,  W = R23 * diag(1, 1, e^{i dcp}),
+//   H_r = O diag(0, dm21, dm31) O^T - fac e0 e0^T,  O = R13 R12  (real)
+//
+// so that every per-layer propagator is A_l = W V_l D_l V_l^T W^dagger with a
+// real orthogonal V_l and D_l = diag(1, e^{i psi1}, e^{i psi2}) (phases
+// relative to the first eigenvalue; a per-layer global phase drops out of
+// |amplitude|^2).  The layer chain of physics.hpp:645-677 then becomes
+//
+//   S_r = B^T A_M B A_0,   B = A_{M-1} ... A_1   (A_l symmetric in this basis)
+//       = V_1 (Y^T D_M Y) T_0 D_0 V_0^T,  Y = T_{M-1} D_{M-1} ... T_1 D_1,
+//   T_l = V_{l+1}^T V_l,
+//
+// which needs about half the complex 3x3 products of the reference chain.
+#pragma once
+
+#include <cstdint>
+
+namespace cp3 {
+
+// constants.hpp:28-40 and physics.hpp:442
+constexpr double kGF = 1.52588e-4;  // 2*sqrt(2)*G_F in the reference's units
+constexpr double kKm2Cm = 1.0e5;
+constexpr double kREarth = 6371.0;
+constexpr double kLoEfac = 2.534;
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+
+constexpr int kMaxRows = 64;        // density rows accepted by set_density
+constexpr int kPhaseTabN = 256;     // entries per turn of the Q1.30 cos/sin table
+constexpr int kMixedWords = 13;     // 32-bit words per (energy, layer) mixed entry
+constexpr int kFp64Words = 11;      // doubles per (energy, layer) FP64 entry
+constexpr int kPerEWords = 18;      // V_0 and V_1 (row-major) per energy
+
+// Oscillation parameters derived on the host from setMNSMatrix and
+// setNeutrinoMasses (propagator.hpp:191-248), passed by value to kernels.
+struct OscParams {
+    double dm01, dm02;   // DM(0,1), DM(0,2) incl. the degeneracy break
+    double d1, d2;       // DM(1,0), DM(2,0): vacuum masses relative to m1
+    double u00, u01, u02;  // |U(0,j)|^2 as the reference forms them
+    double o[9];         // O = R13 R12, row-major
+    double s23, c23, sd, cd;
+    int anti;            // 1 for antineutrinos: sign of the matter term flips
+};
+
+// One problem for the kernels (device pointers).
+struct Problem {
+    int n_cos, n_en;
+    int n_en_pad;        // energies padded to the energy tile
+    int te;              // energies per tile (table tiling and block.x)
+    int nl;              // layers: 1 (vacuum) + density rows
+    int nl_pad;          // row stride of the per-cosine tables
+    const double* energies;  // [n_en]
+    const double* cosines;   // [n_cos]
+    const int* maxlayers;    // [n_cos]
+    const double* radii;     // [nl-1] descending (outermost first)
+    const double* rhoye;     // [nl] layer 0 = 0 (vacuum), layer l = rho*Ye of row l-1
+    double height_cm;
+};
+
+}  // namespace cp3

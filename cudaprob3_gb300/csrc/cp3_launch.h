@@ -1,0 +1,37 @@
+// Host-side launch interface of the propagator kernels (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+#include "cp3_internal.h"
+
+namespace cp3 {
+
+struct PrepArgs {
+    Problem pb;
+    OscParams osc;
+    void* tab;  // per-(energy, layer) table, tile-major
+    void* pe;   // per-energy V_0, V_1
+    void* len;  // per-(cosine, layer) lengths
+};
+
+struct PropArgs {
+    const void* tab;
+    const void* pe;
+    const void* len;
+    const int* maxl;
+    const int2* ptab;  // mixed: 257 Q1.30 (cos, sin) of 2*pi*j/256, j = -128..128
+    void* out;
+    int n_cos, n_en, n_en_pad, nl, nl_pad, cchunk;
+    double c23, s23, cd, sd;     // FP64 flavour rotation
+    int q_c23, q_s23, q_cd, q_sd;  // the same in Q1.30
+};
+
+size_t propagate_smem_bytes(bool mixed, int te, int nl, int nl_pad, int cchunk);
+cudaError_t launch_prep(bool mixed, const PrepArgs& a, cudaStream_t s);
+cudaError_t launch_propagate(bool mixed, const PropArgs& a, int te, int groups, size_t smem,
+                             cudaStream_t s);
+
+}  // namespace cp3

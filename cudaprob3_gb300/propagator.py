@@ -1,0 +1,172 @@
+"""Python mirror of the reference's propagator interface.
+
+``CudaPropagatorSingle`` keeps the names, argument meaning and error
+behaviour of cudaprob3::CudaPropagatorSingle<FLOAT_T> (cudapropagator.cuh:39-251)
+and its base cudaprob3::Propagator<FLOAT_T> (propagator.hpp:43-337); every call
+goes through the C ABI of libcudaprob3_gb300.so.  ``precision`` plays the role
+of FLOAT_T: "fp64" is the plain FP64 method (double results), "mixed" the FP64
+eigen-solve / 32-bit bulk method (float results).
+"""
+import ctypes
+import enum
+
+import numpy as np
+
+from . import _lib
+from ._lib import CP3Error, check
+
+
+class NeutrinoType(enum.IntEnum):
+    """types.hpp:29"""
+    Neutrino = 0
+    Antineutrino = 1
+
+
+class ProbType(enum.IntEnum):
+    """types.hpp:23-27: index = in*3 + out, x_y is P(x -> y)."""
+    e_e = 0
+    e_m = 1
+    e_t = 2
+    m_e = 3
+    m_m = 4
+    m_t = 5
+    t_e = 6
+    t_m = 7
+    t_t = 8
+
+
+Neutrino = NeutrinoType.Neutrino
+Antineutrino = NeutrinoType.Antineutrino
+
+_PRECISIONS = {"fp64": _lib.PRECISION_FP64, "double": _lib.PRECISION_FP64,
+               "mixed": _lib.PRECISION_MIXED, "float": _lib.PRECISION_MIXED}
+
+
+def _dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def device_count():
+    return int(_lib.load().cp3_device_count())
+
+
+class CudaPropagatorSingle:
+    """Single-GPU propagator: CudaPropagatorSingle(id, n_cosines, n_energies)."""
+
+    def __init__(self, device_id, n_cosines, n_energies=None, precision="fp64"):
+        if n_energies is None:  # CudaPropagatorSingle(n_cosines, n_energies) on device 0
+            device_id, n_cosines, n_energies = 0, device_id, n_cosines
+        if precision not in _PRECISIONS:
+            raise ValueError("precision must be one of %s" % sorted(_PRECISIONS))
+        self._lib = _lib.load()
+        self._h = ctypes.c_void_p()
+        check(self._lib.cp3_create(ctypes.byref(self._h), int(device_id), int(n_cosines), int(n_energies),
+                                   _PRECISIONS[precision]))
+        self.device_id = int(device_id)
+        self.n_cosines = int(n_cosines)
+        self.n_energies = int(n_energies)
+        self.precision = "fp64" if _PRECISIONS[precision] == _lib.PRECISION_FP64 else "mixed"
+        self.dtype = np.float64 if self.precision == "fp64" else np.float32
+
+    # -- lifetime -------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.cp3_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- Propagator<FLOAT_T> setters (propagator.hpp:117-286) ------------------
+    def setEnergyList(self, energies):
+        e = np.ascontiguousarray(energies, dtype=np.float64)
+        check(self._lib.cp3_set_energy_list(self._h, _dptr(e), int(e.size)))
+
+    def setCosineList(self, cosines):
+        c = np.ascontiguousarray(cosines, dtype=np.float64)
+        check(self._lib.cp3_set_cosine_list(self._h, _dptr(c), int(c.size)))
+
+    def setMNSMatrix(self, theta12, theta13, theta23, dcp):
+        check(self._lib.cp3_set_mns_matrix(self._h, float(theta12), float(theta13), float(theta23), float(dcp)))
+
+    def setNeutrinoMasses(self, dm12sq, dm23sq):
+        check(self._lib.cp3_set_neutrino_masses(self._h, float(dm12sq), float(dm23sq)))
+
+    def setDensity(self, radii, rhos, ye=None):
+        """Shell table as in propagator.hpp:117-161; ``ye`` (electron fraction
+        per row) defaults to the reference's fixed 0.5."""
+        r = np.ascontiguousarray(radii, dtype=np.float64)
+        d = np.ascontiguousarray(rhos, dtype=np.float64)
+        if r.size != d.size:
+            raise CP3Error(_lib.ERR_ARGUMENT, "setDensity : rhos.size() != radii.size()")
+        y = None if ye is None else np.ascontiguousarray(ye, dtype=np.float64)
+        if y is not None and y.size != r.size:
+            raise CP3Error(_lib.ERR_ARGUMENT, "setDensity : ye.size() != radii.size()")
+        check(self._lib.cp3_set_density(self._h, _dptr(r), _dptr(d), None if y is None else _dptr(y),
+                                        int(r.size)))
+
+    def setDensityFromFile(self, filename):
+        check(self._lib.cp3_set_density_from_file(self._h, str(filename).encode()))
+
+    def setProductionHeight(self, height_km):
+        check(self._lib.cp3_set_production_height(self._h, float(height_km)))
+
+    # -- calculation (cudapropagator.cuh:162-235) -----------------------------
+    def calculateProbabilities(self, ntype):
+        check(self._lib.cp3_calculate_probabilities(self._h, int(ntype)))
+
+    def calculateProbabilitiesAsync(self, ntype):
+        check(self._lib.cp3_calculate_probabilities_async(self._h, int(ntype)))
+
+    def waitForCompletion(self):
+        check(self._lib.cp3_wait_for_completion(self._h))
+
+    def getProbability(self, index_cosine, index_energy, t):
+        out = ctypes.c_double()
+        check(self._lib.cp3_get_probability(self._h, int(index_cosine), int(index_energy), int(t),
+                                            ctypes.byref(out)))
+        return out.value
+
+    # -- bulk access (no reference counterpart) -------------------------------
+    def result_bytes(self):
+        n = ctypes.c_size_t()
+        check(self._lib.cp3_result_bytes(self._h, ctypes.byref(n)))
+        return n.value
+
+    def result_device_ptr(self):
+        p = ctypes.c_void_p()
+        check(self._lib.cp3_result_device_ptr(self._h, ctypes.byref(p)))
+        return p.value
+
+    def results(self, out=None):
+        """All probabilities as [9][n_cosines][n_energies] (plane in*3+out)."""
+        shape = (9, self.n_cosines, self.n_energies)
+        if out is None:
+            out = np.empty(shape, dtype=self.dtype)
+        if out.dtype != self.dtype or out.shape != shape or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous %s array of shape %s" % (self.dtype, shape))
+        check(self._lib.cp3_copy_results_to_host(self._h, out.ctypes.data_as(ctypes.c_void_p), out.nbytes))
+        return out
+
+    def copy_results_to(self, host_ptr, nbytes):
+        check(self._lib.cp3_copy_results_to_host(self._h, ctypes.c_void_p(host_ptr), int(nbytes)))
+
+    def set_result_buffer(self, device_ptr, nbytes):
+        check(self._lib.cp3_set_result_buffer(self._h, ctypes.c_void_p(device_ptr), int(nbytes)))
+
+    def set_stream(self, stream_handle):
+        check(self._lib.cp3_set_stream(self._h, ctypes.c_void_p(stream_handle)))
+
+    def last_launch_count(self):
+        n = ctypes.c_int()
+        check(self._lib.cp3_last_launch_count(self._h, ctypes.byref(n)))
+        return n.value

@@ -1,0 +1,143 @@
+/*
+ * cudaprob3_gb300 -- C ABI of the GB300 (sm_103a) Barger propagator.
+ *
+ * This is the drop-in boundary for CUDAProb3++'s single-GPU path: every entry
+ * point below replaces one member of cudaprob3::CudaPropagatorSingle<FLOAT_T>
+ * (cudapropagator.cuh:39-251) or of its base cudaprob3::Propagator<FLOAT_T>
+ * (propagator.hpp:43-337).  The citation beside each declaration names the
+ * reference member it replaces.  The C++ classes in include/cudaprob3/ wrap
+ * this ABI with the reference's own class names and signatures.
+ *
+ * Conventions
+ *   - Plain C types only: pointers, sizes, doubles.  Host arrays are read
+ *     during the call and not retained.
+ *   - Every function returns CP3_OK (0) or a negative status.  The message of
+ *     the last failure on the calling thread is returned by cp3_last_error().
+ *     Where the reference throws std::runtime_error the same message text is
+ *     used; where it calls exit(1) on a CUDA error (hpc_helpers.cuh:70-82)
+ *     this ABI returns CP3_ERR_CUDA instead.
+ *   - Each handle owns its device buffers, its stream and its parameters; no
+ *     process-global physics state exists (the reference keeps its mixing
+ *     data in globals, physics.hpp:114-124), so distinct handles may be used
+ *     from distinct host threads.  One handle must not be used by two host
+ *     threads at once.
+ *   - Results live on the device in the reference's GPU layout: 9 planes
+ *     [in*3+out][n_cosines][n_energies] (physics.hpp:689-691).  The element
+ *     type is double for CP3_PRECISION_FP64 and float for CP3_PRECISION_MIXED.
+ */
+#ifndef CUDAPROB3_GB300_H
+#define CUDAPROB3_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CP3_ABI_VERSION 1
+
+/* status codes */
+#define CP3_OK 0
+#define CP3_ERR_ARGUMENT (-1)  /* bad size, index, pointer or value          */
+#define CP3_ERR_STATE (-2)     /* call order violated / input not yet set     */
+#define CP3_ERR_CUDA (-3)      /* CUDA runtime failure                         */
+#define CP3_ERR_NO_DEVICE (-4) /* no GPU, or the device id does not exist     */
+#define CP3_ERR_FILE (-5)      /* density file could not be opened            */
+#define CP3_ERR_LIMIT (-6)     /* a size exceeds a documented limit           */
+
+/* arithmetic of a propagator */
+#define CP3_PRECISION_FP64 0  /* plain method: every step in FP64              */
+#define CP3_PRECISION_MIXED 1 /* FP64 eigen-solve, 32-bit bulk, float results */
+
+/* NeutrinoType, types.hpp:29 */
+#define CP3_NEUTRINO 0
+#define CP3_ANTINEUTRINO 1
+
+/* ProbType index = in*3+out, types.hpp:23-27 */
+
+typedef struct cp3_propagator cp3_propagator;
+
+/* Version of this ABI (CP3_ABI_VERSION). */
+int cp3_abi_version(void);
+
+/* Message of the last failure on this thread ("" when none). */
+const char* cp3_last_error(void);
+
+/* Number of visible CUDA devices (0 when none); never fails. */
+int cp3_device_count(void);
+
+/* CudaPropagatorSingle(int id, int n_cosines, int n_energies),
+ * cudapropagator.cuh:50-80; `precision` selects the arithmetic. */
+int cp3_create(cp3_propagator** out, int device_id, int n_cosines, int n_energies,
+               int precision);
+
+/* ~CudaPropagatorSingle(), cudapropagator.cuh:91-94.  NULL is accepted. */
+int cp3_destroy(cp3_propagator* p);
+
+/* Propagator::setEnergyList, propagator.hpp:252-257 (GeV); n must equal n_energies. */
+int cp3_set_energy_list(cp3_propagator* p, const double* energies, int n);
+
+/* Propagator::setCosineList, propagator.hpp:261-274; n must equal n_cosines. */
+int cp3_set_cosine_list(cp3_propagator* p, const double* cosines, int n);
+
+/* Propagator::setMNSMatrix, propagator.hpp:191-221 (radians). */
+int cp3_set_mns_matrix(cp3_propagator* p, double theta12, double theta13, double theta23,
+                       double dcp);
+
+/* Propagator::setNeutrinoMasses, propagator.hpp:226-248 (eV^2). */
+int cp3_set_neutrino_masses(cp3_propagator* p, double dm12sq, double dm23sq);
+
+/* Propagator::setDensity, propagator.hpp:117-161 (km, g/cm^3), extended by an
+ * electron fraction per row.  `ye` may be NULL: every row then uses 0.5, the
+ * reference's fixed factor (constants.hpp:40).  Rows: 1..CP3_MAX_ROWS. */
+int cp3_set_density(cp3_propagator* p, const double* radii, const double* rhos,
+                    const double* ye, int n);
+#define CP3_MAX_ROWS 64
+
+/* Propagator::setDensityFromFile, propagator.hpp:169-184 (two columns). */
+int cp3_set_density_from_file(cp3_propagator* p, const char* path);
+
+/* Propagator::setProductionHeight, propagator.hpp:279-286 (km). */
+int cp3_set_production_height(cp3_propagator* p, double height_km);
+
+/* CudaPropagatorSingle::calculateProbabilities, cudapropagator.cuh:162-165
+ * (launch and wait).  type: CP3_NEUTRINO or CP3_ANTINEUTRINO. */
+int cp3_calculate_probabilities(cp3_propagator* p, int type);
+
+/* CudaPropagatorSingle::calculateProbabilitiesAsync, cudapropagator.cuh:191-220. */
+int cp3_calculate_probabilities_async(cp3_propagator* p, int type);
+
+/* CudaPropagatorSingle::waitForCompletion, cudapropagator.cuh:223-226. */
+int cp3_wait_for_completion(cp3_propagator* p);
+
+/* CudaPropagatorSingle::getProbability, cudapropagator.cuh:168-181.  The first
+ * call after a calculation copies all 9 planes to pinned host memory. */
+int cp3_get_probability(cp3_propagator* p, int index_cosine, int index_energy,
+                        int prob_type, double* out);
+
+/* Device pointer of the result planes (no reference counterpart: the
+ * reference keeps d_result_list private, cudapropagator.cuh:245). */
+int cp3_result_device_ptr(cp3_propagator* p, void** dptr);
+
+/* Size in bytes of the result planes: 9 * n_cosines * n_energies * element. */
+int cp3_result_bytes(cp3_propagator* p, size_t* bytes);
+
+/* Copy all result planes to host memory `dst` of `bytes` bytes
+ * (cudapropagator.cuh:229-235 without the lazy flag). */
+int cp3_copy_results_to_host(cp3_propagator* p, void* dst, size_t bytes);
+
+/* Write results into a caller-owned device buffer (>= cp3_result_bytes) from
+ * the next calculation on; NULL returns to the handle's own buffer. */
+int cp3_set_result_buffer(cp3_propagator* p, void* dptr, size_t bytes);
+
+/* Run on a caller-owned cudaStream_t (NULL returns to the handle's own stream). */
+int cp3_set_stream(cp3_propagator* p, void* cuda_stream);
+
+/* Kernel launches issued by the last calculation (all are this library's). */
+int cp3_last_launch_count(cp3_propagator* p, int* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUDAPROB3_GB300_H */

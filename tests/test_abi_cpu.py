@@ -1,0 +1,58 @@
+"""The C ABI library without a GPU: it loads, exports every declared symbol,
+and reports errors through status codes."""
+import ctypes
+import os
+import re
+
+import pytest
+
+import cudaprob3_gb300 as cp
+from cudaprob3_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADERS = [os.path.join(ROOT, "include", "cudaprob3_gb300.h")]
+
+
+def declared_symbols():
+    names = set()
+    for h in HEADERS:
+        text = open(h).read()
+        names |= set(re.findall(r"^\s*(?:int|const char\*)\s+(cp3_\w+)\s*\(", text, re.M))
+    return sorted(names)
+
+
+def test_library_loads():
+    lib = cp.load_library()
+    assert lib.cp3_abi_version() == 1
+
+
+@pytest.mark.parametrize("name", declared_symbols())
+def test_symbol_exported(name):
+    lib = ctypes.CDLL(_lib.LIB_PATH)
+    assert hasattr(lib, name)
+
+
+def test_binding_covers_header():
+    bound = {n for n, _, _ in _lib.SIGNATURES}
+    assert set(declared_symbols()) <= bound
+
+
+def test_null_handle_errors():
+    lib = cp.load_library()
+    assert lib.cp3_set_production_height(None, 1.0) == _lib.ERR_ARGUMENT
+    assert b"null" in lib.cp3_last_error()
+    assert lib.cp3_destroy(None) == 0
+
+
+def test_create_without_device():
+    if cp.device_count() > 0:
+        pytest.skip("a device is visible")
+    with pytest.raises(cp.CP3Error) as e:
+        cp.CudaPropagatorSingle(0, 8, 8)
+    assert e.value.code == _lib.ERR_NO_DEVICE
+    assert "No GPU found" in str(e.value)
+
+
+def test_bad_precision_rejected():
+    with pytest.raises(ValueError):
+        cp.CudaPropagatorSingle(0, 8, 8, precision="half")
