@@ -1,0 +1,424 @@
+"""Throughput benchmark of the GB300 Barger propagator.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (one step): the 4096-cosine x 4096-energy grid (cosines uniform in
+[-1, 0], energies log-spaced over 0.1-1000 GeV), 11-shell PREM body with
+electron fractions 0.468 (core) / 0.497 (mantle), nominal oscillation point,
+production height 22 km, computed for neutrinos AND antineutrinos (two
+calculateProbabilities calls, 2 x 16.8M pairs).  Metric: (cos, E) pairs/s.
+
+Our arm runs the mixed-precision kernel (FP64 eigen-solve, Q1.30 fixed-point
+chain, float results) and reports beside it the plain FP64 kernel on the same
+workload, the precision of mixed against FP64 (every pair) and against the
+oracle (strided subset), the roofline of the dominant kernel and the CPU
+baseline.  The reference arm times the reference's CPU path (the oracle's C
+restatement of CpuPropagator<double>, all host threads) on a bounded sample of
+the same workload.
+
+N > 1 (torchrun): every rank runs the same workload on its own GPU (replicas,
+weak scaling; the path has no exchange step); value = all ranks' pairs / the
+slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NC = NE = 4096
+E_MIN, E_MAX = 0.1, 1000.0
+WORKLOAD = ("4096 cos x 4096 E (cos in [-1,0], 0.1-1000 GeV log), 11-shell PREM "
+            "(Ye 0.468 core / 0.497 mantle), nominal parameters, h=22 km, nu + nubar per step")
+METRIC = "(cos,E) pairs/s on 1 GB300: mixed-precision vs plain FP64 at max|dP|<=1e-6"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-seconds", type=float, default=8.0, help="target CPU time of the baseline sample")
+    ap.add_argument("--skip-fp64", action="store_true")
+    return ap.parse_args()
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(world, x):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def grid():
+    from cudaprob3_gb300 import grids as G
+    return G.linspace(-1.0, 0.0, NC), G.logspace(E_MIN, E_MAX, NE), G.PREM_12, G.NOMINAL
+
+
+# ------------------------------------------------------------- work units --
+def madw_per_pair(M):
+    """mad.wide.s32 operations one pair executes in the mixed kernel
+    (cp3_chain.cuh): 8 per layer phase pair, 78 per inner chain step, and the
+    fixed cost of G, K, the two eigen-basis products and the flavour rotation."""
+    M = np.asarray(M, dtype=np.int64)
+    return np.where(M >= 2, 86 * M + 210, np.where(M == 1, 362, 120))
+
+
+def survey_flops_per_pair(M):
+    """Per-pair algorithmic work of the reference formulation,
+    F = (M+1)*(3 + 216 + 3) + n_mm*216 + 27 with n_mm = 2M (M >= 1) or 1."""
+    M = np.asarray(M, dtype=np.int64)
+    nmm = np.where(M >= 1, 2 * M, 1)
+    return (M + 1) * 222 + nmm * 216 + 27
+
+
+# ------------------------------------------------------------------ clocks --
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            import tempfile
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        power = [float(r[3]) for r in rows if r[3].replace(".", "").isdigit()]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows), "power_w_max": max(power) if power else None}
+
+
+# -------------------------------------------------------------- CPU legs --
+def cpu_sample(target_s, threads=0):
+    """Time the oracle (CpuPropagator<double> restated) on whole cosine rows of
+    the workload, nu and nubar alternately, until about `target_s` seconds.
+    Returns (pairs/s, threads, description)."""
+    import oracle
+    cos, en, B, nom = grid()
+    threads = threads or os.cpu_count() or 1
+    rows = 0
+    pairs = 0
+    t_total = 0.0
+    k = 0
+    while t_total < target_s and k < NC // 16:
+        c = cos[(np.arange(16) * (NC // 16) + k) % NC]
+        t0 = time.perf_counter()
+        oracle.calculate(c, en, B.radii, B.rho_eff(), nom, 22.0, bool(k % 2), threads=threads)
+        t_total += time.perf_counter() - t0
+        pairs += c.size * en.size
+        rows += c.size
+        k += 1
+    desc = "%d cosine rows x %d energies (strided over the grid, nu/nubar alternating), %.1f s" % (
+        rows, NE, t_total)
+    return pairs / t_total, threads, desc
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    import oracle
+    cos, en, B, nom = grid()
+    threads = os.cpu_count() or 1
+    rows_per_step = 16
+    times = []
+    for s in range(args.warmup + args.steps):
+        c = cos[(np.arange(rows_per_step) * (NC // rows_per_step) + s) % NC]
+        t0 = time.perf_counter()
+        for anti in (False, True):
+            oracle.calculate(c, en, B.radii, B.rho_eff(), nom, 22.0, anti, threads=threads)
+        dt = time.perf_counter() - t0
+        if s >= args.warmup:
+            times.append(dt)
+    pairs = 2 * rows_per_step * NE * len(times)
+    value = pairs / sum(times)
+    sample = ("per step: %d cosine rows x %d energies, nu and nubar (%d pairs of the 2x16.8M)"
+              % (rows_per_step, NE, 2 * rows_per_step * NE))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "sample": sample},
+            "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------- ours --
+def make_prop(cp, precision, cos, en, B, nom, device):
+    p = cp.CudaPropagatorSingle(device, len(cos), len(en), precision=precision)
+    p.setEnergyList(en)
+    p.setCosineList(cos)
+    p.setMNSMatrix(*nom[:4])
+    p.setNeutrinoMasses(*nom[4:])
+    p.setDensity(B.radii, B.rhos, B.ye)
+    p.setProductionHeight(22.0)
+    return p
+
+
+def run_ours(args, world, rank, local):
+    import torch
+
+    import cudaprob3_gb300 as cp
+    from cudaprob3_gb300 import _lib
+    from cudaprob3_gb300.propagator import pipe_peak
+
+    dev = local
+    torch.cuda.set_device(dev)
+    cos, en, B, nom = grid()
+    stream = torch.cuda.Stream(device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+
+    def build(precision):
+        props = []
+        bufs = []
+        dt = torch.float32 if precision == "mixed" else torch.float64
+        for anti in (False, True):
+            p = make_prop(cp, precision, cos, en, B, nom, dev)
+            buf = torch.empty((9, NC, NE), dtype=dt, device=dev)
+            p.set_result_buffer(buf.data_ptr(), buf.numel() * buf.element_size())
+            p.set_stream(stream.cuda_stream)
+            props.append((p, cp.Antineutrino if anti else cp.Neutrino))
+            bufs.append(buf)
+        return props, bufs
+
+    def timed_steps(props, steps, warmup, kernel_times=None):
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                for p, t in props:
+                    p.calculateProbabilitiesAsync(t)
+            stream.synchronize()
+            evs = []
+            barrier(world)
+            torch.cuda.synchronize()
+            for _ in range(steps):
+                flush.zero_()
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                for p, t in props:
+                    p.calculateProbabilitiesAsync(t)
+                b.record(stream)
+                evs.append((a, b))
+                if kernel_times is not None:
+                    for p, _ in props:
+                        kernel_times.append(p.last_kernel_ms())
+            torch.cuda.synchronize()
+            barrier(world)
+        return [a.elapsed_time(b) for a, b in evs]
+
+    # ---- mixed: the headline
+    props, bufs = build("mixed")
+    for p, _ in props:
+        p.set_kernel_timing(True)
+    maxl = props[0][0].maxlayers()
+    sampler = ClockSampler(dev)
+    kt = []
+    sampler.start()
+    times = timed_steps(props, args.steps, args.warmup, kt)
+    clocks = sampler.stop()
+    for p, _ in props:
+        p.set_kernel_timing(False)
+    ms_step = allmax(world, sum(times) / len(times))
+    pairs_step = 2 * NC * NE
+    value = world * pairs_step / (ms_step * 1e-3)
+    launches = sum(p.last_launch_count() for p, _ in props) * args.steps
+
+    prop_ms = float(np.mean([k[1] for k in kt]))
+    prep_ms = float(np.mean([k[0] for k in kt]))
+    madw = float(madw_per_pair(maxl).sum()) * NE
+    peak_madw = pipe_peak(_lib.PIPE_IMAD_WIDE, dev)
+    peak_ffma = pipe_peak(_lib.PIPE_FFMA, dev)
+    peak_dfma = pipe_peak(_lib.PIPE_DFMA, dev)
+    out_bytes = 9 * NC * NE * 4
+    survey_f = float(survey_flops_per_pair(maxl).sum()) * NE
+    try:
+        mp = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        hbm_peak, hbm_src = float(mp["hbm_gbs"]), "MEASURED_PEAKS.json (measured)"
+    except (OSError, KeyError, ValueError):
+        hbm_peak, hbm_src = 6800.0, "fallback 6.8 TB/s"
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "propagate_mixed_traffic.json")
+    if os.path.exists(tp):
+        try:
+            traffic = json.load(open(tp)).get("dram_bytes_per_launch_at_4096x4096")
+        except ValueError:
+            traffic = None
+    roofline = {
+        "bound": "fma-pipe (mad.wide.s32 integer MAC on the FMA-heavy pipe)",
+        "achieved": madw / (prop_ms * 1e-3) / 1e12, "peak": peak_madw / 1e12, "unit": "Tops/s",
+        "frac": (madw / (prop_ms * 1e-3)) / peak_madw, "traffic": traffic,
+        "kernel": "propagate_kernel<mixed>", "kernel_ms": prop_ms, "prep_kernel_ms": prep_ms,
+        "work_per_launch": madw, "peak_source": "measured live on this GPU (cp3_pipe_peak)",
+        "hbm_output_gbs": out_bytes / (prop_ms * 1e-3) / 1e9, "hbm_peak_gbs": hbm_peak,
+        "hbm_frac": out_bytes / (prop_ms * 1e-3) / 1e9 / hbm_peak, "hbm_peak_source": hbm_src,
+        "survey_equiv_tflops": survey_f / (prop_ms * 1e-3) / 1e12,
+        "ffma_peak_tflops": 2 * peak_ffma / 1e12, "dfma_peak_tflops": 2 * peak_dfma / 1e12,
+    }
+
+    # ---- e2e through the public API with host buffers
+    host = [torch.empty((9, NC, NE), dtype=torch.float32, pin_memory=True) for _ in props]
+    cos_h = np.ascontiguousarray(cos)
+    en_h = np.ascontiguousarray(en)
+    e2e_steps = max(3, min(args.steps, 20))
+    for p, _ in props:
+        p.set_result_buffer(0, 0)
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for (p, t), h in zip(props, host):
+            p.setEnergyList(en_h)
+            p.setCosineList(cos_h)
+            p.calculateProbabilities(t)
+            p.copy_results_to(h.data_ptr(), h.numel() * 4)
+    torch.cuda.synchronize()
+    e2e_s = allmax(world, (time.perf_counter() - t0) / e2e_steps)
+    e2e = {"value": world * pairs_step / e2e_s, "unit": "pairs/s",
+           "h2d_bytes_per_step": 2 * 8 * (NC + NE), "d2h_bytes_per_step": 2 * out_bytes,
+           "ms_per_step": e2e_s * 1e3}
+    for (p, _), buf in zip(props, bufs):
+        p.set_result_buffer(buf.data_ptr(), buf.numel() * 4)
+
+    # ---- plain FP64 on the same workload
+    fp64 = None
+    prec = {}
+    if not args.skip_fp64:
+        fprops, fbufs = build("fp64")
+        fsteps = max(1, min(args.steps, 3))
+        ftimes = timed_steps(fprops, fsteps, 1)
+        fms = allmax(world, sum(ftimes) / len(ftimes))
+        fp64 = {"value": world * pairs_step / (fms * 1e-3), "unit": "pairs/s", "ms_per_step": fms,
+                "steps": fsteps}
+        # precision of this step's mixed results against FP64 (every pair)
+        for p, t in props:
+            p.calculateProbabilitiesAsync(t)
+        stream.synchronize()
+        dmax, dsum = 0.0, 0.0
+        for bm, bf in zip(bufs, fbufs):
+            d = (bm.double() - bf).abs()
+            dmax = max(dmax, float(d.max()))
+            dsum += float(d.mean())
+        prec = {"max_abs_dp_vs_fp64": dmax, "mean_abs_dp_vs_fp64": dsum / len(bufs)}
+        for p, _ in fprops:
+            p.close()
+        del fbufs
+    if rank == 0:
+        import oracle
+        idx = np.arange(0, NC, 32)
+        err = 0.0
+        mean = 0.0
+        for k, (p, t) in enumerate(props):
+            want = oracle.calculate(cos[idx], en[idx], B.radii, B.rho_eff(), nom, 22.0, bool(t))
+            got = bufs[k].cpu().numpy()[:, idx][:, :, idx].astype(np.float64)
+            err = max(err, float(np.abs(got - want).max()))
+            mean += float(np.abs(got - want).mean()) / 2
+        prec["max_abs_dp_vs_oracle_subset"] = err
+        prec["mean_abs_dp_vs_oracle_subset"] = mean
+        prec["oracle_subset"] = "every 32nd cosine x every 32nd energy (128 x 128), nu and nubar"
+
+    cpu = None
+    if rank == 0 and world == 1:
+        v, thr, desc = cpu_sample(args.cpu_seconds)
+        cpu = {"value": v, "unit": "pairs/s", "cores": thr, "kind": "port", "sample": desc}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "i32 Q1.30 chain + f32 phases + f64 eigen-solve (float out)",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "precision": "mixed", "pairs_per_step": pairs_step,
+                       "l2": "flushed between steps (256 MB write outside the timed events); "
+                             "outputs 2 x 604 MB per step exceed L2",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clocks, "fp64": fp64, "precision": prec,
+            "speedup_vs_fp64": (value / fp64["value"]) if fp64 else None,
+        }
+        print(json.dumps(line), flush=True)
+    for p, _ in props:
+        p.close()
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_init(args)
+    try:
+        if args.impl == "reference":
+            run_reference(args, world, rank)
+        else:
+            run_ours(args, world, rank, local)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -51,7 +51,15 @@ SIGNATURES = [
     ("cp3_set_result_buffer", _I, [_P, _P, _SZ]),
     ("cp3_set_stream", _I, [_P, _P]),
     ("cp3_last_launch_count", _I, [_P, _IP]),
+    ("cp3_get_maxlayers", _I, [_P, _IP, _I]),
+    ("cp3_set_kernel_timing", _I, [_P, _I]),
+    ("cp3_last_kernel_ms", _I, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+    ("cp3_pipe_peak", _I, [_I, _I, _DP]),
 ]
+
+PIPE_IMAD_WIDE = 0
+PIPE_FFMA = 1
+PIPE_DFMA = 2
 
 _lib = None
 

@@ -97,6 +97,10 @@ struct cp3_propagator {
     // launch shape
     int te = 64, groups = 4, cchunk = 32;
 
+    // optional per-kernel timing
+    bool timing = false;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+
     size_t elem() const { return mixed ? sizeof(float) : sizeof(double); }
     size_t result_bytes() const { return (size_t)9 * n_cos * n_en * elem(); }
     void* result_ptr() const { return ext_result ? ext_result : (void*)d_result.p; }
@@ -212,6 +216,8 @@ int cp3_destroy(cp3_propagator* p) {
     p->d_result.release();
     p->d_ptab.release();
     if (p->h_result) cudaFreeHost(p->h_result);
+    for (auto& e : p->ev)
+        if (e) cudaEventDestroy(e);
     if (p->own_stream) cudaStreamDestroy(p->own_stream);
     delete p;
     return CP3_OK;
@@ -469,7 +475,9 @@ int cp3_calculate_probabilities_async(cp3_propagator* p, int type) {
     pa.tab = p->d_tab.p;
     pa.pe = p->d_pe.p;
     pa.len = p->d_len.p;
+    if (p->timing && (e = cudaEventRecord(p->ev[0], p->stream)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
     if ((e = cp3::launch_prep(p->mixed, pa, p->stream)) != cudaSuccess) return cuda_fail(e, "prep kernel");
+    if (p->timing && (e = cudaEventRecord(p->ev[1], p->stream)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
 
     cp3::PropArgs ka{};
     ka.tab = p->d_tab.p;
@@ -494,6 +502,7 @@ int cp3_calculate_probabilities_async(cp3_propagator* p, int type) {
     ka.q_sd = (int)std::llround(ka.sd * 1073741824.0);
     if ((e = cp3::launch_propagate(p->mixed, ka, te, groups, smem, p->stream)) != cudaSuccess)
         return cuda_fail(e, "propagate kernel");
+    if (p->timing && (e = cudaEventRecord(p->ev[2], p->stream)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
     p->last_launches = 2;
     return CP3_OK;
 }
@@ -565,6 +574,51 @@ int cp3_last_launch_count(cp3_propagator* p, int* launches) {
     if (int rc = check(p)) return rc;
     if (!launches) return fail(CP3_ERR_ARGUMENT, "null output pointer");
     *launches = p->last_launches;
+    return CP3_OK;
+}
+
+int cp3_get_maxlayers(cp3_propagator* p, int* out, int n) {
+    if (int rc = check(p)) return rc;
+    if (n != p->n_cos || (n > 0 && !out)) return fail(CP3_ERR_ARGUMENT, "get_maxlayers: n must equal n_cosines");
+    std::copy(p->maxlayers.begin(), p->maxlayers.end(), out);
+    return CP3_OK;
+}
+
+int cp3_set_kernel_timing(cp3_propagator* p, int enable) {
+    if (int rc = check(p)) return rc;
+    DeviceGuard g(p->device);
+    if (enable && !p->ev[0]) {
+        for (auto& e : p->ev) {
+            cudaError_t err = cudaEventCreate(&e);
+            if (err != cudaSuccess) return cuda_fail(err, "cudaEventCreate");
+        }
+    }
+    p->timing = enable != 0;
+    return CP3_OK;
+}
+
+int cp3_last_kernel_ms(cp3_propagator* p, float* prep_ms, float* prop_ms) {
+    if (int rc = check(p)) return rc;
+    if (!p->timing || p->last_launches == 0) return fail(CP3_ERR_STATE, "last_kernel_ms: no timed calculation");
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaEventSynchronize(p->ev[2]);
+    float a = 0, b = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&a, p->ev[0], p->ev[1]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&b, p->ev[1], p->ev[2]);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaEventElapsedTime");
+    if (prep_ms) *prep_ms = a;
+    if (prop_ms) *prop_ms = b;
+    return CP3_OK;
+}
+
+int cp3_pipe_peak(int device, int pipe, double* ops) {
+    if (!ops) return fail(CP3_ERR_ARGUMENT, "null output pointer");
+    if (pipe < 0 || pipe > 2) return fail(CP3_ERR_ARGUMENT, "unknown pipe");
+    if (device < 0 || device >= cp3_device_count()) return fail(CP3_ERR_NO_DEVICE, "No GPU found");
+    DeviceGuard g(device);
+    if (g.err != cudaSuccess) return cuda_fail(g.err, "cudaSetDevice");
+    cudaError_t e = cp3::measure_pipe(pipe, ops);
+    if (e != cudaSuccess) return cuda_fail(e, "pipe probe");
     return CP3_OK;
 }
 

@@ -34,4 +34,7 @@ cudaError_t launch_prep(bool mixed, const PrepArgs& a, cudaStream_t s);
 cudaError_t launch_propagate(bool mixed, const PropArgs& a, int te, int groups, size_t smem,
                              cudaStream_t s);
 
+// Throughput of one pipe on the current device (0 mad.wide.s32, 1 FFMA, 2 DFMA).
+cudaError_t measure_pipe(int pipe, double* ops_per_second);
+
 }  // namespace cp3

@@ -50,6 +50,13 @@ def device_count():
     return int(_lib.load().cp3_device_count())
 
 
+def pipe_peak(pipe, device_id=0):
+    """Measured operations per second of one pipe (_lib.PIPE_*) on a device."""
+    out = ctypes.c_double()
+    check(_lib.load().cp3_pipe_peak(int(device_id), int(pipe), ctypes.byref(out)))
+    return out.value
+
+
 class CudaPropagatorSingle:
     """Single-GPU propagator: CudaPropagatorSingle(id, n_cosines, n_energies)."""
 
@@ -165,6 +172,21 @@ class CudaPropagatorSingle:
 
     def set_stream(self, stream_handle):
         check(self._lib.cp3_set_stream(self._h, ctypes.c_void_p(stream_handle)))
+
+    def maxlayers(self):
+        out = np.empty(self.n_cosines, dtype=np.int32)
+        check(self._lib.cp3_get_maxlayers(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                          self.n_cosines))
+        return out
+
+    def set_kernel_timing(self, enable=True):
+        check(self._lib.cp3_set_kernel_timing(self._h, 1 if enable else 0))
+
+    def last_kernel_ms(self):
+        """(prep_ms, propagate_ms) of the last timed calculation."""
+        a, b = ctypes.c_float(), ctypes.c_float()
+        check(self._lib.cp3_last_kernel_ms(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     def last_launch_count(self):
         n = ctypes.c_int()

@@ -136,6 +136,24 @@ int cp3_set_stream(cp3_propagator* p, void* cuda_stream);
 /* Kernel launches issued by the last calculation (all are this library's). */
 int cp3_last_launch_count(cp3_propagator* p, int* launches);
 
+/* Layers crossed per cosine (Propagator::maxlayers, propagator.hpp:301-307). */
+int cp3_get_maxlayers(cp3_propagator* p, int* out, int n);
+
+/* Record CUDA events around each kernel of the following calculations
+ * (0 disables); cp3_last_kernel_ms returns the durations of the last one. */
+int cp3_set_kernel_timing(cp3_propagator* p, int enable);
+int cp3_last_kernel_ms(cp3_propagator* p, float* prep_ms, float* propagate_ms);
+
+/* Measured throughput of one GPU pipe on `device`, in operations per second
+ * (no reference counterpart; it gives the roofline denominators):
+ *   CP3_PIPE_IMAD_WIDE  mad.wide.s32 (32x32+64 -> 64), the Q1.30 chain's MAC
+ *   CP3_PIPE_FFMA       FP32 fused multiply-add
+ *   CP3_PIPE_DFMA       FP64 fused multiply-add                                */
+#define CP3_PIPE_IMAD_WIDE 0
+#define CP3_PIPE_FFMA 1
+#define CP3_PIPE_DFMA 2
+int cp3_pipe_peak(int device, int pipe, double* ops_per_second);
+
 #ifdef __cplusplus
 }
 #endif

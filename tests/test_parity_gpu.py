@@ -2,7 +2,9 @@
 of the reference and against the oracle on full grids.
 
 Tolerances (max |dP| over all nine channels):
-  fp64  1e-11  (the degenerate dm21 = 0 case: 1e-9; its eigenvalue gap is 5e-9 eV^2)
+  fp64  1e-11  (the degenerate dm21 = 0 and dm32 = 0 cases: 1e-9; the reference's
+               degeneracy break leaves an eigenvalue gap of 5e-9 eV^2, and both the
+               reference and this library lose accuracy as eps*|H|/gap there)
   mixed 1e-6
 """
 import os
@@ -38,7 +40,7 @@ def run(cp, precision, cos, en, radii, rhos, ye, params, h=22.0, anti=False):
 
 
 def tol_for(name, precision):
-    if precision == "fp64" and "dm12_zero" in name:
+    if precision == "fp64" and ("dm12_zero" in name or "dm23_zero" in name):
         return 1e-9
     return TOL[precision]
 
