@@ -41,7 +41,7 @@ def test_cpp_dropin_runs_like_reference_example(gpu):
         dens = os.path.join(d, "prem12.dat")
         with open(dens, "w") as f:
             for r, rho in zip(G.PREM_12.radii, G.PREM_12.rhos):
-                f.write("%r %r\n" % (r, rho))
+                f.write("%.17g %.17g\n" % (r, rho))
         out = os.path.join(d, "out.bin")
         r = subprocess.run([exe, out, dens], capture_output=True, text=True)
         assert r.returncode == 0, r.stderr

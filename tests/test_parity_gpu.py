@@ -156,7 +156,7 @@ def test_density_from_file(gpu):
         path = os.path.join(d, "prem4.dat")
         with open(path, "w") as f:
             for r, rho in zip(G.PREM_4.radii, G.PREM_4.rhos):
-                f.write("%r %r\n" % (r, rho))
+                f.write("%.17g %.17g\n" % (r, rho))
         with make(gpu, "fp64", c, e, G.PREM_4.radii, G.PREM_4.rhos, None, G.NOMINAL) as p:
             p.calculateProbabilities(gpu.Neutrino)
             a = p.results()
