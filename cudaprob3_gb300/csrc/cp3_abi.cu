@@ -84,7 +84,7 @@ struct cp3_propagator {
     DevBuf<double> d_energy, d_cosine, d_radii, d_rhoye;
     DevBuf<int> d_maxl;
     DevBuf<unsigned char> d_tab, d_pe, d_len, d_result;
-    DevBuf<int2> d_ptab;
+    DevBuf<int4> d_ptab;
     void* ext_result = nullptr;
     size_t ext_bytes = 0;
     bool maxl_dirty = true, energy_dirty = true, cosine_dirty = true, density_dirty = true;
@@ -185,15 +185,20 @@ int cp3_create(cp3_propagator** out, int device_id, int n_cosines, int n_energie
     if ((e = p->d_result.ensure(std::max<size_t>(p->result_bytes(), 16))) != cudaSuccess)
         return bail(e, "cudaMalloc");
     if (p->mixed) {
-        // Q1.30 cos/sin of 2*pi*j/256, j = -128..128
-        std::vector<int2> tab(cp3::kPhaseTabN + 1);
+        // cos/sin of 2*pi*j/256, j = -128..128, in Q1.30 and as float
+        std::vector<int4> tab(cp3::kPhaseTabN + 1);
         for (int j = -cp3::kPhaseTabN / 2; j <= cp3::kPhaseTabN / 2; j++) {
             const double ang = cp3::kTwoPi * j / cp3::kPhaseTabN;
-            tab[j + cp3::kPhaseTabN / 2] = make_int2((int)std::llround(std::cos(ang) * 1073741824.0),
-                                                      (int)std::llround(std::sin(ang) * 1073741824.0));
+            const double c = std::cos(ang), s = std::sin(ang);
+            float cf = (float)c, sf = (float)s;
+            int ci, si;
+            std::memcpy(&ci, &cf, 4);
+            std::memcpy(&si, &sf, 4);
+            tab[j + cp3::kPhaseTabN / 2] =
+                make_int4((int)std::llround(c * 1073741824.0), (int)std::llround(s * 1073741824.0), ci, si);
         }
         if ((e = p->d_ptab.ensure(tab.size())) != cudaSuccess) return bail(e, "cudaMalloc");
-        if ((e = cudaMemcpy(p->d_ptab.p, tab.data(), tab.size() * sizeof(int2), cudaMemcpyHostToDevice)) !=
+        if ((e = cudaMemcpy(p->d_ptab.p, tab.data(), tab.size() * sizeof(int4), cudaMemcpyHostToDevice)) !=
             cudaSuccess)
             return bail(e, "cudaMemcpy");
     }
@@ -419,7 +424,7 @@ int cp3_calculate_probabilities_async(cp3_propagator* p, int type) {
     size_t smem = cp3::propagate_smem_bytes(p->mixed, te, nl, nl_pad, cchunk);
     while (smem > 227 * 1024 && te > 32) {
         te /= 2;
-        groups = std::min(groups * 2, 256 / te);
+        groups = std::min(groups * 2, cp3::propagate_max_threads(p->mixed) / te);
         smem = cp3::propagate_smem_bytes(p->mixed, te, nl, nl_pad, cchunk);
     }
     while (smem > 227 * 1024 && cchunk > 8) {
@@ -500,6 +505,7 @@ int cp3_calculate_probabilities_async(cp3_propagator* p, int type) {
     ka.q_s23 = (int)std::llround(ka.s23 * 1073741824.0);
     ka.q_cd = (int)std::llround(ka.cd * 1073741824.0);
     ka.q_sd = (int)std::llround(ka.sd * 1073741824.0);
+    ka.bias = 1LL << 29;
     if ((e = cp3::launch_propagate(p->mixed, ka, te, groups, smem, p->stream)) != cudaSuccess)
         return cuda_fail(e, "propagate kernel");
     if (p->timing && (e = cudaEventRecord(p->ev[2], p->stream)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");

@@ -18,63 +18,63 @@
 namespace cp3 {
 
 // ---------------------------------------------------------------- Q1.30 ----
+// Instances carry the rounding bias 2^29 in a register pair (it is loaded from
+// a kernel argument, so it is neither folded nor rematerialised per use).
 struct Q30 {
     using R = int;
     struct C {
         int re, im;
     };
-    static constexpr long long kBias = 1LL << 29;  // round-half-up on >> 30
+    long long bias;    // 1 << 29: round half up on the final >> 30
 
     static __device__ __forceinline__ long long mad(int a, int b, long long c) {
         long long d;
         asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
         return d;
     }
-    static __device__ __forceinline__ int rnd(long long acc) { return (int)(acc >> 30); }
+    // bits 30..61 of a 64-bit accumulator: one funnel shift
+    static __device__ __forceinline__ int rnd(long long acc) {
+        int r;
+        asm("{\n\t.reg .b32 lo, hi;\n\tmov.b64 {lo, hi}, %1;\n\tshf.r.clamp.b32 %0, lo, hi, 30;\n\t}"
+            : "=r"(r)
+            : "l"(acc));
+        return r;
+    }
 
     static __device__ __forceinline__ R one() { return 1 << 30; }
     static __device__ __forceinline__ C cz() { return C{0, 0}; }
     static __device__ __forceinline__ C creal(R x) { return C{x, 0}; }
+    static __device__ __forceinline__ C conj(C z) { return C{z.re, -z.im}; }
 
     // t * z  (real times complex)
-    static __device__ __forceinline__ C mulRC(R t, C z) {
-        return C{rnd(mad(t, z.re, kBias)), rnd(mad(t, z.im, kBias))};
-    }
-    // a * b
-    static __device__ __forceinline__ C mulCC(C a, C b) {
-        long long r = mad(a.re, b.re, kBias);
-        r = mad(-a.im, b.im, r);
-        long long i = mad(a.re, b.im, kBias);
-        i = mad(a.im, b.re, i);
-        return C{rnd(r), rnd(i)};
-    }
+    __device__ __forceinline__ C mulRC(R t, C z) const { return C{rnd(mad(t, z.re, bias)), rnd(mad(t, z.im, bias))}; }
     // z * e where e = (c, s) and ns = -s is supplied to save a negation
-    static __device__ __forceinline__ C mulPhase(C z, int c, int s, int ns) {
-        long long r = mad(z.re, c, kBias);
+    __device__ __forceinline__ C mulPhase(C z, int c, int s, int ns) const {
+        long long r = mad(z.re, c, bias);
         r = mad(z.im, ns, r);
-        long long i = mad(z.im, c, kBias);
+        long long i = mad(z.im, c, bias);
         i = mad(z.re, s, i);
         return C{rnd(r), rnd(i)};
     }
     // t0 z0 + t1 z1 + t2 z2
-    static __device__ __forceinline__ C dotRC(R t0, R t1, R t2, C z0, C z1, C z2) {
-        long long r = mad(t0, z0.re, kBias);
+    __device__ __forceinline__ C dotRC(R t0, R t1, R t2, C z0, C z1, C z2) const {
+        long long r = mad(t0, z0.re, bias);
         r = mad(t1, z1.re, r);
         r = mad(t2, z2.re, r);
-        long long i = mad(t0, z0.im, kBias);
+        long long i = mad(t0, z0.im, bias);
         i = mad(t1, z1.im, i);
         i = mad(t2, z2.im, i);
         return C{rnd(r), rnd(i)};
     }
     // a0 b0 + a1 b1 + a2 b2 (complex)
-    static __device__ __forceinline__ C dotCC(C a0, C a1, C a2, C b0, C b1, C b2) {
-        long long r = mad(a0.re, b0.re, kBias);
+    __device__ __forceinline__ C dotCC(C a0, C a1, C a2, C b0, C b1, C b2) const {
+        long long r = mad(a0.re, b0.re, bias);
         r = mad(-a0.im, b0.im, r);
         r = mad(a1.re, b1.re, r);
         r = mad(-a1.im, b1.im, r);
         r = mad(a2.re, b2.re, r);
         r = mad(-a2.im, b2.im, r);
-        long long i = mad(a0.re, b0.im, kBias);
+        long long i = mad(a0.re, b0.im, bias);
         i = mad(a0.im, b0.re, i);
         i = mad(a1.re, b1.im, i);
         i = mad(a1.im, b1.re, i);
@@ -83,16 +83,32 @@ struct Q30 {
         return C{rnd(r), rnd(i)};
     }
     // c*x + s*y  and  -s*x + c*y  for a real rotation of two complex numbers
-    static __device__ __forceinline__ void rot(R c, R s, C& x, C& y) {
-        const C nx{rnd(mad(s, y.re, mad(c, x.re, kBias))), rnd(mad(s, y.im, mad(c, x.im, kBias)))};
-        const C ny{rnd(mad(c, y.re, mad(-s, x.re, kBias))), rnd(mad(c, y.im, mad(-s, x.im, kBias)))};
+    __device__ __forceinline__ void rot(R c, R s, C& x, C& y) const {
+        const int ns = -s;
+        const C nx{rnd(mad(s, y.re, mad(c, x.re, bias))), rnd(mad(s, y.im, mad(c, x.im, bias)))};
+        const C ny{rnd(mad(c, y.re, mad(ns, x.re, bias))), rnd(mad(c, y.im, mad(ns, x.im, bias)))};
         x = nx;
         y = ny;
     }
-    static __device__ __forceinline__ float prob(C z) {
-        const float a = __int2float_rn(z.re) * (1.0f / 1073741824.0f);
-        const float b = __int2float_rn(z.im) * (1.0f / 1073741824.0f);
-        return fmaf(a, a, b * b);
+    // |z|^2 exactly, as Q2.60 in 64 bits
+    static __device__ __forceinline__ long long norm2(C z) { return mad(z.im, z.im, mad(z.re, z.re, 0LL)); }
+    // Q2.60 probability -> float, one rounding; the completed entries of the
+    // doubly stochastic matrix may come out a few 1e-10 below zero: clamp
+    static __device__ __forceinline__ float to_prob(long long q) {
+        return q <= 0 ? 0.0f : __ll2float_rn(q) * 8.673617379884035e-19f;  // 2^-60
+    }
+    // the nine probabilities from the 2x2 block B = (S[e][e], S[e][mu], S[mu][e], S[mu][mu])
+    // of a unitary S: out[in*3+out] = |S[out][in]|^2, rows and columns summing to one
+    static __device__ __forceinline__ void complete(const C B[4], float out[9]) {
+        const long long one = 1LL << 60;
+        const long long q00 = norm2(B[0]), q01 = norm2(B[1]), q10 = norm2(B[2]), q11 = norm2(B[3]);
+        // q[out][in]
+        const long long q02 = one - q00 - q01, q12 = one - q10 - q11;
+        const long long q20 = one - q00 - q10, q21 = one - q01 - q11;
+        const long long q22 = q00 + q01 + q10 + q11 - one;
+        out[0] = to_prob(q00); out[1] = to_prob(q10); out[2] = to_prob(q20);
+        out[3] = to_prob(q01); out[4] = to_prob(q11); out[5] = to_prob(q21);
+        out[6] = to_prob(q02); out[7] = to_prob(q12); out[8] = to_prob(q22);
     }
 };
 
@@ -104,10 +120,14 @@ struct Q30 {
 //      so t = integer + j/256 + d with |d| <= 1/512 (+ rounding);
 //   3. x = 2 pi d; sin x = x - x^3/6 and cos x - 1 = -x^2/2 + x^4/24 in FP32
 //      (truncation below 3e-12 for |x| <= pi/256);
-//   4. rotate the table entry (cos, sin)(2 pi j/256) by x in Q1.30.
-// `tab` holds 257 pairs (Q1.30 cos, sin) for j = -128..128 at index j + 128.
+//   4. rotate the table entry (C, S) = (cos, sin)(2 pi j/256) by x: the
+//      corrections C (cos x - 1) - S sin x and S (cos x - 1) + C sin x are
+//      below 0.013 in magnitude, so FP32 carries them to ~1e-9 absolute, and
+//      they are added to the exact Q1.30 table entry.
+// `tab` holds 257 entries (Q1.30 cos, Q1.30 sin, float cos, float sin) for
+// j = -128..128 at index j + 128.
 __device__ __forceinline__ void phase_q30(float kh, float kl, float Lh, float Ll,
-                                          const int2* __restrict__ tab, int& cq, int& sq) {
+                                          const int4* __restrict__ tab, int& cq, int& sq) {
     const float p = kh * Lh;
     float e = fmaf(kh, Lh, -p);
     e = fmaf(kh, Ll, e);
@@ -121,15 +141,12 @@ __device__ __forceinline__ void phase_q30(float kh, float kl, float Lh, float Ll
     const float x2 = x * x;
     const float sx = x * fmaf(x2, -0.16666666666666666f, 1.0f);
     const float cm = x2 * fmaf(x2, 0.041666666666666664f, -0.5f);
-    const int isx = __float2int_rn(sx * 1073741824.0f);
-    const int icm = __float2int_rn(cm * 1073741824.0f);
-    const int2 cs = tab[(int)j + 128];
-    long long ac = Q30::mad(cs.x, icm, Q30::kBias);
-    ac = Q30::mad(-cs.y, isx, ac);
-    long long as = Q30::mad(cs.y, icm, Q30::kBias);
-    as = Q30::mad(cs.x, isx, as);
-    cq = cs.x + Q30::rnd(ac);
-    sq = cs.y + Q30::rnd(as);
+    const int4 t = tab[(int)j + 128];
+    const float cf = __int_as_float(t.z), sf = __int_as_float(t.w);
+    const float dc = fmaf(cf, cm, -sf * sx);
+    const float ds = fmaf(sf, cm, cf * sx);
+    cq = t.x + __float2int_rn(dc * 1073741824.0f);
+    sq = t.y + __float2int_rn(ds * 1073741824.0f);
 }
 
 // ------------------------------------------------------------------ FP64 ----
@@ -141,6 +158,7 @@ struct F64 {
     static __device__ __forceinline__ R one() { return 1.0; }
     static __device__ __forceinline__ C cz() { return C{0.0, 0.0}; }
     static __device__ __forceinline__ C creal(R x) { return C{x, 0.0}; }
+    static __device__ __forceinline__ C conj(C z) { return C{z.re, -z.im}; }
     static __device__ __forceinline__ C mulRC(R t, C z) { return C{t * z.re, t * z.im}; }
     static __device__ __forceinline__ C mulCC(C a, C b) {
         return C{fma(a.re, b.re, -a.im * b.im), fma(a.re, b.im, a.im * b.re)};
@@ -172,7 +190,16 @@ struct F64 {
         x = nx;
         y = ny;
     }
-    static __device__ __forceinline__ double prob(C z) { return fma(z.re, z.re, z.im * z.im); }
+    static __device__ __forceinline__ void complete(const C B[4], double out[9]) {
+        const double q00 = fma(B[0].re, B[0].re, B[0].im * B[0].im), q01 = fma(B[1].re, B[1].re, B[1].im * B[1].im);
+        const double q10 = fma(B[2].re, B[2].re, B[2].im * B[2].im), q11 = fma(B[3].re, B[3].re, B[3].im * B[3].im);
+        const double q02 = 1.0 - q00 - q01, q12 = 1.0 - q10 - q11;
+        const double q20 = 1.0 - q00 - q10, q21 = 1.0 - q01 - q11;
+        const double q22 = q00 + q01 + q10 + q11 - 1.0;
+        out[0] = q00; out[1] = q10; out[2] = fmax(q20, 0.0);
+        out[3] = q01; out[4] = q11; out[5] = fmax(q21, 0.0);
+        out[6] = fmax(q02, 0.0); out[7] = fmax(q12, 0.0); out[8] = fmax(q22, 0.0);
+    }
 };
 
 // FP64 cos/sin of 2*pi*t, t = kappa * L turns.

@@ -10,8 +10,10 @@
 //   S_r = V_1 (Y^T D_M Y) T_0 D_0 V_0^T,   Y = T_{M-1} D_{M-1} ... T_1 D_1,
 //
 // with T_l = V_{l+1}^T V_l.  M = 0 (cos >= 0, atmosphere only, physics.hpp:562)
-// gives S_r = V_0 D_0 V_0^T.  Finally S_f = W S_r W^dagger and
-// P(in -> out) = |S_f[out][in]|^2 (physics.hpp:682-691).
+// gives S_r = V_0 D_0 V_0^T.  The flavour amplitude is S_f = W S_r W^dagger and
+// P(in -> out) = |S_f[out][in]|^2 (physics.hpp:682-691); W enters only through
+// the per-energy tables Lambda' = rows e, mu of W V_1 and
+// Gamma' = columns e, mu of V_0^T W^dagger.
 #pragma once
 
 #include "cp3_arith.cuh"
@@ -20,32 +22,44 @@ namespace cp3 {
 
 // Src provides, for the current pair:
 //   void phase(int l, R& c1, R& s1, R& n1, R& c2, R& s2, R& n2)  e^{i psi_k}, n = -s
-//   R T(int l, int i, int j)    overlap V_{l+1}^T V_l
-//   R V0(int i, int j), V1(int i, int j)
+//   R T(int l, int i, int j)     overlap V_{l+1}^T V_l
+//   R La(int j)                  row 0 of W V_1 (real)
+//   C Lb(int j)                  row 1 of W V_1
+//   R Ga(int k)                  column 0 of V_0^T W^dagger (real)
+//   C Gb(int k)                  column 1 of V_0^T W^dagger
+//
+// Only the 2x2 block S_f[out][in], out, in in {e, mu}, is formed: S_f is
+// unitary, so the 3x3 matrix of |S_f|^2 is doubly stochastic and its other
+// five entries follow from this block (complete_probabilities).
 template <class P, class Src>
-__device__ __forceinline__ void real_basis_amplitude(const Src& src, int M, typename P::C S[9]) {
+__device__ __forceinline__ void flavour_block(const P& ar, const Src& src, int M, typename P::C B[4]) {
     using R = typename P::R;
     using C = typename P::C;
     R c1, s1, n1, c2, s2, n2;
+    // X' = T_0 D_0 Gamma' (3x2), or D_0 Gamma' when only the atmosphere is crossed
+    src.phase(0, c1, s1, n1, c2, s2, n2);
+    C g0[3], g1[3];  // D_0 Gamma': columns 0 and 1
+    g0[0] = P::creal(src.Ga(0));
+    g0[1] = ar.mulRC(src.Ga(1), C{c1, s1});
+    g0[2] = ar.mulRC(src.Ga(2), C{c2, s2});
+    g1[0] = src.Gb(0);
+    g1[1] = ar.mulPhase(src.Gb(1), c1, s1, n1);
+    g1[2] = ar.mulPhase(src.Gb(2), c2, s2, n2);
     if (M == 0) {
-        src.phase(0, c1, s1, n1, c2, s2, n2);
-        C X[9];  // X[3j+k] = V0(j,k) D_k
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            X[3 * j] = P::creal(src.V0(j, 0));
-            X[3 * j + 1] = P::mulRC(src.V0(j, 1), C{c1, s1});
-            X[3 * j + 2] = P::mulRC(src.V0(j, 2), C{c2, s2});
-        }
-#pragma unroll
-        for (int i = 0; i < 3; i++)
-#pragma unroll
-            for (int j = i; j < 3; j++) {
-                const C v = P::dotRC(src.V0(i, 0), src.V0(i, 1), src.V0(i, 2), X[3 * j], X[3 * j + 1],
-                                     X[3 * j + 2]);
-                S[3 * i + j] = v;
-                S[3 * j + i] = v;
-            }
+        // S_r = V_0 D_0 V_0^T, so the block is Gamma'^dagger (D_0 Gamma')
+        const C a0 = P::creal(src.Ga(0)), a1 = P::creal(src.Ga(1)), a2 = P::creal(src.Ga(2));
+        const C b0 = P::conj(src.Gb(0)), b1 = P::conj(src.Gb(1)), b2 = P::conj(src.Gb(2));
+        B[0] = ar.dotCC(a0, a1, a2, g0[0], g0[1], g0[2]);
+        B[1] = ar.dotCC(a0, a1, a2, g1[0], g1[1], g1[2]);
+        B[2] = ar.dotCC(b0, b1, b2, g0[0], g0[1], g0[2]);
+        B[3] = ar.dotCC(b0, b1, b2, g1[0], g1[1], g1[2]);
         return;
+    }
+    C x0[3], x1[3];  // T_0 (D_0 Gamma')
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        x0[i] = ar.dotRC(src.T(0, i, 0), src.T(0, i, 1), src.T(0, i, 2), g0[0], g0[1], g0[2]);
+        x1[i] = ar.dotRC(src.T(0, i, 0), src.T(0, i, 1), src.T(0, i, 2), g1[0], g1[1], g1[2]);
     }
     C Y[9];
     if (M >= 2) {
@@ -53,8 +67,8 @@ __device__ __forceinline__ void real_basis_amplitude(const Src& src, int M, type
 #pragma unroll
         for (int i = 0; i < 3; i++) {
             Y[3 * i] = P::creal(src.T(1, i, 0));
-            Y[3 * i + 1] = P::mulRC(src.T(1, i, 1), C{c1, s1});
-            Y[3 * i + 2] = P::mulRC(src.T(1, i, 2), C{c2, s2});
+            Y[3 * i + 1] = ar.mulRC(src.T(1, i, 1), C{c1, s1});
+            Y[3 * i + 2] = ar.mulRC(src.T(1, i, 2), C{c2, s2});
         }
         for (int l = 2; l < M; l++) {
             src.phase(l, c1, s1, n1, c2, s2, n2);
@@ -64,11 +78,11 @@ __device__ __forceinline__ void real_basis_amplitude(const Src& src, int M, type
 #pragma unroll
             for (int j = 0; j < 3; j++) {
                 const C z0 = Y[j];
-                const C z1 = P::mulPhase(Y[3 + j], c1, s1, n1);
-                const C z2 = P::mulPhase(Y[6 + j], c2, s2, n2);
-                Y[j] = P::dotRC(t00, t01, t02, z0, z1, z2);
-                Y[3 + j] = P::dotRC(t10, t11, t12, z0, z1, z2);
-                Y[6 + j] = P::dotRC(t20, t21, t22, z0, z1, z2);
+                const C z1 = ar.mulPhase(Y[3 + j], c1, s1, n1);
+                const C z2 = ar.mulPhase(Y[6 + j], c2, s2, n2);
+                Y[j] = ar.dotRC(t00, t01, t02, z0, z1, z2);
+                Y[3 + j] = ar.dotRC(t10, t11, t12, z0, z1, z2);
+                Y[6 + j] = ar.dotRC(t20, t21, t22, z0, z1, z2);
             }
         }
     } else {
@@ -84,69 +98,28 @@ __device__ __forceinline__ void real_basis_amplitude(const Src& src, int M, type
 #pragma unroll
         for (int j = 0; j < 3; j++) {
             Z[j] = Y[j];
-            Z[3 + j] = P::mulPhase(Y[3 + j], c1, s1, n1);
-            Z[6 + j] = P::mulPhase(Y[6 + j], c2, s2, n2);
+            Z[3 + j] = ar.mulPhase(Y[3 + j], c1, s1, n1);
+            Z[6 + j] = ar.mulPhase(Y[6 + j], c2, s2, n2);
         }
         int g = 0;
 #pragma unroll
         for (int i = 0; i < 3; i++)
 #pragma unroll
-            for (int j = i; j < 3; j++) G[g++] = P::dotCC(Y[i], Y[3 + i], Y[6 + i], Z[j], Z[3 + j], Z[6 + j]);
+            for (int j = i; j < 3; j++) G[g++] = ar.dotCC(Y[i], Y[3 + i], Y[6 + i], Z[j], Z[3 + j], Z[6 + j]);
     }
-    // K = G T_0 D_0
-    src.phase(0, c1, s1, n1, c2, s2, n2);
-    C K[9];
-    {
-        const C g00 = G[0], g01 = G[1], g02 = G[2], g11 = G[3], g12 = G[4], g22 = G[5];
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            const R a = src.T(0, 0, j), b = src.T(0, 1, j), c = src.T(0, 2, j);
-            C k0 = P::dotRC(a, b, c, g00, g01, g02);
-            C k1 = P::dotRC(a, b, c, g01, g11, g12);
-            C k2 = P::dotRC(a, b, c, g02, g12, g22);
-            if (j == 1) {
-                k0 = P::mulPhase(k0, c1, s1, n1);
-                k1 = P::mulPhase(k1, c1, s1, n1);
-                k2 = P::mulPhase(k2, c1, s1, n1);
-            } else if (j == 2) {
-                k0 = P::mulPhase(k0, c2, s2, n2);
-                k1 = P::mulPhase(k1, c2, s2, n2);
-                k2 = P::mulPhase(k2, c2, s2, n2);
-            }
-            K[j] = k0;
-            K[3 + j] = k1;
-            K[6 + j] = k2;
-        }
-    }
-    // S_r = V_1 K V_0^T
-    C S1[9];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++)
-            S1[3 * i + j] = P::dotRC(src.V1(i, 0), src.V1(i, 1), src.V1(i, 2), K[j], K[3 + j], K[6 + j]);
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++)
-            S[3 * i + j] = P::dotRC(src.V0(j, 0), src.V0(j, 1), src.V0(j, 2), S1[3 * i], S1[3 * i + 1],
-                                    S1[3 * i + 2]);
-}
-
-// S_f = W S_r W^dagger with W = R23 diag(1, 1, e^{i dcp}), in place.
-template <class P>
-__device__ __forceinline__ void to_flavour(typename P::C S[9], typename P::R c23, typename P::R s23,
-                                           typename P::R cd, typename P::R sd) {
-    // diag(1,1,e^{i d}) S diag(1,1,e^{-i d})
-    S[6] = P::mulPhase(S[6], cd, sd, -sd);
-    S[7] = P::mulPhase(S[7], cd, sd, -sd);
-    S[2] = P::mulPhase(S[2], cd, -sd, sd);
-    S[5] = P::mulPhase(S[5], cd, -sd, sd);
-    // R23 from the left (rows 1, 2), then R23^T from the right (columns 1, 2)
-#pragma unroll
-    for (int j = 0; j < 3; j++) P::rot(c23, s23, S[3 + j], S[6 + j]);
-#pragma unroll
-    for (int i = 0; i < 3; i++) P::rot(c23, s23, S[3 * i + 1], S[3 * i + 2]);
+    // X = G X' (3x2)
+    C X0[3], X1[3];
+    X0[0] = ar.dotCC(G[0], G[1], G[2], x0[0], x0[1], x0[2]);
+    X0[1] = ar.dotCC(G[1], G[3], G[4], x0[0], x0[1], x0[2]);
+    X0[2] = ar.dotCC(G[2], G[4], G[5], x0[0], x0[1], x0[2]);
+    X1[0] = ar.dotCC(G[0], G[1], G[2], x1[0], x1[1], x1[2]);
+    X1[1] = ar.dotCC(G[1], G[3], G[4], x1[0], x1[1], x1[2]);
+    X1[2] = ar.dotCC(G[2], G[4], G[5], x1[0], x1[1], x1[2]);
+    // block = Lambda' X: row 0 of W V_1 is real, row 1 complex
+    B[0] = ar.dotRC(src.La(0), src.La(1), src.La(2), X0[0], X0[1], X0[2]);
+    B[1] = ar.dotRC(src.La(0), src.La(1), src.La(2), X1[0], X1[1], X1[2]);
+    B[2] = ar.dotCC(src.Lb(0), src.Lb(1), src.Lb(2), X0[0], X0[1], X0[2]);
+    B[3] = ar.dotCC(src.Lb(0), src.Lb(1), src.Lb(2), X1[0], X1[1], X1[2]);
 }
 
 }  // namespace cp3

@@ -34,9 +34,10 @@ constexpr double kTwoPi = 6.283185307179586476925286766559;
 
 constexpr int kMaxRows = 64;        // density rows accepted by set_density
 constexpr int kPhaseTabN = 256;     // entries per turn of the Q1.30 cos/sin table
+constexpr int kPhaseTabBytes = (kPhaseTabN + 1) * 16;  // int4 per entry
 constexpr int kMixedWords = 13;     // 32-bit words per (energy, layer) mixed entry
 constexpr int kFp64Words = 11;      // doubles per (energy, layer) FP64 entry
-constexpr int kPerEWords = 18;      // V_0 and V_1 (row-major) per energy
+constexpr int kPerEWords = 18;      // Lambda' and Gamma' per energy (see cp3_chain.cuh)
 
 // Oscillation parameters derived on the host from setMNSMatrix and
 // setNeutrinoMasses (propagator.hpp:191-248), passed by value to kernels.

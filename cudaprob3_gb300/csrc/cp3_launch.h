@@ -15,6 +15,7 @@ struct PrepArgs {
     void* tab;  // per-(energy, layer) table, tile-major
     void* pe;   // per-energy V_0, V_1
     void* len;  // per-(cosine, layer) lengths
+    int n_energy_blocks;  // set by launch_prep
 };
 
 struct PropArgs {
@@ -22,7 +23,8 @@ struct PropArgs {
     const void* pe;
     const void* len;
     const int* maxl;
-    const int2* ptab;  // mixed: 257 Q1.30 (cos, sin) of 2*pi*j/256, j = -128..128
+    const int4* ptab;  // mixed: 257 (Q1.30 cos, Q1.30 sin, float cos, float sin) of 2*pi*j/256
+    long long bias;    // 1 << 29, the rounding constant of the Q1.30 path
     void* out;
     int n_cos, n_en, n_en_pad, nl, nl_pad, cchunk;
     double c23, s23, cd, sd;     // FP64 flavour rotation
@@ -30,7 +32,10 @@ struct PropArgs {
 };
 
 size_t propagate_smem_bytes(bool mixed, int te, int nl, int nl_pad, int cchunk);
-cudaError_t launch_prep(bool mixed, const PrepArgs& a, cudaStream_t s);
+
+// Largest block (threads) the propagate kernel of a precision accepts.
+inline int propagate_max_threads(bool mixed) { return mixed ? 256 : 128; }
+cudaError_t launch_prep(bool mixed, PrepArgs a, cudaStream_t s);
 cudaError_t launch_propagate(bool mixed, const PropArgs& a, int te, int groups, size_t smem,
                              cudaStream_t s);
 

@@ -9,6 +9,8 @@ namespace cp3 {
 
 constexpr int kProbeIters = 4096;
 
+// The multiplier changes every iteration so that no product can be hoisted
+// out of the loop (a loop-invariant product turns the loop into 64-bit adds).
 __global__ void probe_imad_wide(long long* out, int a) {
     long long x[8];
     int y[8];
@@ -16,9 +18,11 @@ __global__ void probe_imad_wide(long long* out, int a) {
         x[i] = threadIdx.x + i;
         y[i] = threadIdx.x * 7 + i;
     }
+    int z = a;
     for (int it = 0; it < kProbeIters; it++) {
+        z ^= it;
 #pragma unroll
-        for (int i = 0; i < 8; i++) asm volatile("mad.wide.s32 %0, %1, %2, %0;" : "+l"(x[i]) : "r"(y[i]), "r"(a));
+        for (int i = 0; i < 8; i++) asm volatile("mad.wide.s32 %0, %1, %2, %0;" : "+l"(x[i]) : "r"(y[i]), "r"(z));
     }
     long long s = 0;
     for (int i = 0; i < 8; i++) s += x[i];
@@ -30,7 +34,7 @@ __global__ void probe_ffma(float* out, float a, float b) {
     for (int i = 0; i < 8; i++) x[i] = threadIdx.x * 1e-3f + i;
     for (int it = 0; it < kProbeIters; it++) {
 #pragma unroll
-        for (int i = 0; i < 8; i++) x[i] = fmaf(x[i], a, b);
+        for (int i = 0; i < 8; i++) asm volatile("fma.rn.f32 %0, %0, %1, %2;" : "+f"(x[i]) : "f"(a), "f"(b));
     }
     float s = 0;
     for (int i = 0; i < 8; i++) s += x[i];
@@ -42,7 +46,7 @@ __global__ void probe_dfma(double* out, double a, double b) {
     for (int i = 0; i < 8; i++) x[i] = threadIdx.x * 1e-3 + i;
     for (int it = 0; it < kProbeIters / 16; it++) {
 #pragma unroll
-        for (int i = 0; i < 8; i++) x[i] = fma(x[i], a, b);
+        for (int i = 0; i < 8; i++) asm volatile("fma.rn.f64 %0, %0, %1, %2;" : "+d"(x[i]) : "d"(a), "d"(b));
     }
     double s = 0;
     for (int i = 0; i < 8; i++) s += x[i];
