@@ -91,10 +91,11 @@ def grid():
 # ------------------------------------------------------------- work units --
 def madw_per_pair(M):
     """mad.wide.s32 operations one pair executes in the mixed kernel
-    (cp3_chain.cuh): 8 per layer phase pair, 78 per inner chain step, and the
-    fixed cost of G, K, the two eigen-basis products and the flavour rotation."""
+    (flavour_block in cp3_chain.cuh): 78 per inner chain step T_l D_l, and the
+    fixed cost of D_0 Gamma', T_0 (.), G = Y^T D_M Y, G X', Lambda' X and the
+    four exact |S|^2 of the 2x2 flavour block."""
     M = np.asarray(M, dtype=np.int64)
-    return np.where(M >= 2, 86 * M + 210, np.where(M == 1, 362, 120))
+    return np.where(M >= 2, 78 * M + 116, np.where(M == 1, 260, 68))
 
 
 def survey_flops_per_pair(M):

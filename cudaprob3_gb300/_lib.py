@@ -55,6 +55,25 @@ SIGNATURES = [
     ("cp3_set_kernel_timing", _I, [_P, _I]),
     ("cp3_last_kernel_ms", _I, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     ("cp3_pipe_peak", _I, [_I, _I, _DP]),
+    ("cp3_batch_create", _I, [ctypes.POINTER(_P), _I, _I, _I, _IP, _IP]),
+    ("cp3_batch_destroy", _I, [_P]),
+    ("cp3_batch_set_grids", _I, [_P, _DP, _DP]),
+    ("cp3_batch_set_parameters", _I, [_P, _DP]),
+    ("cp3_batch_set_density", _I, [_P, _DP, _DP, _DP, _I, _DP]),
+    ("cp3_batch_set_production_height", _I, [_P, _D]),
+    ("cp3_batch_set_stream", _I, [_P, _P]),
+    ("cp3_batch_set_launch_shape", _I, [_P, _I, _I, _I]),
+    ("cp3_batch_get_launch_shape", _I, [_P, _IP, _IP, _IP, _IP]),
+    ("cp3_batch_autotune", _I, [_P, _I, _I, _IP, _IP, _IP, ctypes.POINTER(ctypes.c_float)]),
+    ("cp3_batch_calculate", _I, [_P, _I]),
+    ("cp3_batch_calculate_async", _I, [_P, _I]),
+    ("cp3_batch_wait", _I, [_P]),
+    ("cp3_batch_calculate_sequential", _I, [_P, _I]),
+    ("cp3_batch_last_ms", _I, [_P, ctypes.POINTER(ctypes.c_float)]),
+    ("cp3_batch_result_offsets", _I, [_P, ctypes.POINTER(ctypes.c_longlong)]),
+    ("cp3_batch_result_device_ptr", _I, [_P, ctypes.POINTER(_P)]),
+    ("cp3_batch_copy_results_to_host", _I, [_P, _P, _SZ]),
+    ("cp3_batch_get_maxlayers", _I, [_P, _IP, ctypes.c_longlong]),
 ]
 
 PIPE_IMAD_WIDE = 0

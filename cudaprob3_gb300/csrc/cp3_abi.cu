@@ -63,6 +63,10 @@ struct DevBuf {
 
 }  // namespace
 
+namespace cp3 {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace cp3
+
 struct cp3_propagator {
     int device = 0;
     int n_cos = 0, n_en = 0;
@@ -505,7 +509,6 @@ int cp3_calculate_probabilities_async(cp3_propagator* p, int type) {
     ka.q_s23 = (int)std::llround(ka.s23 * 1073741824.0);
     ka.q_cd = (int)std::llround(ka.cd * 1073741824.0);
     ka.q_sd = (int)std::llround(ka.sd * 1073741824.0);
-    ka.bias = 1LL << 29;
     if ((e = cp3::launch_propagate(p->mixed, ka, te, groups, smem, p->stream)) != cudaSuccess)
         return cuda_fail(e, "propagate kernel");
     if (p->timing && (e = cudaEventRecord(p->ev[2], p->stream)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");

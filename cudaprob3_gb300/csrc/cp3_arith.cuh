@@ -18,24 +18,31 @@
 namespace cp3 {
 
 // ---------------------------------------------------------------- Q1.30 ----
-// Instances carry the rounding bias 2^29 in a register pair (it is loaded from
-// a kernel argument, so it is neither folded nor rematerialised per use).
+// Every dot product starts with mul.wide (one IMAD.WIDE) and accumulates with
+// mad.wide into the same register pair (IMAD.WIDE + IADD3); rounding to
+// nearest (half up) takes bits 30..61 with a funnel shift and adds bit 29,
+// all on the ALU pipe, which keeps the FMA-heavy pipe for the products.
 struct Q30 {
     using R = int;
     struct C {
         int re, im;
     };
-    long long bias;    // 1 << 29: round half up on the final >> 30
 
+    static __device__ __forceinline__ long long mul(int a, int b) {
+        long long d;
+        asm("mul.wide.s32 %0, %1, %2;" : "=l"(d) : "r"(a), "r"(b));
+        return d;
+    }
     static __device__ __forceinline__ long long mad(int a, int b, long long c) {
         long long d;
         asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
         return d;
     }
-    // bits 30..61 of a 64-bit accumulator: one funnel shift
+    // round(acc / 2^30), ties up: bits 30..61 plus bit 29
     static __device__ __forceinline__ int rnd(long long acc) {
         int r;
-        asm("{\n\t.reg .b32 lo, hi;\n\tmov.b64 {lo, hi}, %1;\n\tshf.r.clamp.b32 %0, lo, hi, 30;\n\t}"
+        asm("{\n\t.reg .b32 lo, hi, q, b;\n\tmov.b64 {lo, hi}, %1;\n\tshf.r.clamp.b32 q, lo, hi, 30;\n\t"
+            "bfe.u32 b, lo, 29, 1;\n\tadd.s32 %0, q, b;\n\t}"
             : "=r"(r)
             : "l"(acc));
         return r;
@@ -47,34 +54,34 @@ struct Q30 {
     static __device__ __forceinline__ C conj(C z) { return C{z.re, -z.im}; }
 
     // t * z  (real times complex)
-    __device__ __forceinline__ C mulRC(R t, C z) const { return C{rnd(mad(t, z.re, bias)), rnd(mad(t, z.im, bias))}; }
+    __device__ __forceinline__ C mulRC(R t, C z) const { return C{rnd(mul(t, z.re)), rnd(mul(t, z.im))}; }
     // z * e where e = (c, s) and ns = -s is supplied to save a negation
     __device__ __forceinline__ C mulPhase(C z, int c, int s, int ns) const {
-        long long r = mad(z.re, c, bias);
+        long long r = mul(z.re, c);
         r = mad(z.im, ns, r);
-        long long i = mad(z.im, c, bias);
+        long long i = mul(z.im, c);
         i = mad(z.re, s, i);
         return C{rnd(r), rnd(i)};
     }
     // t0 z0 + t1 z1 + t2 z2
     __device__ __forceinline__ C dotRC(R t0, R t1, R t2, C z0, C z1, C z2) const {
-        long long r = mad(t0, z0.re, bias);
+        long long r = mul(t0, z0.re);
         r = mad(t1, z1.re, r);
         r = mad(t2, z2.re, r);
-        long long i = mad(t0, z0.im, bias);
+        long long i = mul(t0, z0.im);
         i = mad(t1, z1.im, i);
         i = mad(t2, z2.im, i);
         return C{rnd(r), rnd(i)};
     }
     // a0 b0 + a1 b1 + a2 b2 (complex)
     __device__ __forceinline__ C dotCC(C a0, C a1, C a2, C b0, C b1, C b2) const {
-        long long r = mad(a0.re, b0.re, bias);
+        long long r = mul(a0.re, b0.re);
         r = mad(-a0.im, b0.im, r);
         r = mad(a1.re, b1.re, r);
         r = mad(-a1.im, b1.im, r);
         r = mad(a2.re, b2.re, r);
         r = mad(-a2.im, b2.im, r);
-        long long i = mad(a0.re, b0.im, bias);
+        long long i = mul(a0.re, b0.im);
         i = mad(a0.im, b0.re, i);
         i = mad(a1.re, b1.im, i);
         i = mad(a1.im, b1.re, i);
@@ -85,13 +92,13 @@ struct Q30 {
     // c*x + s*y  and  -s*x + c*y  for a real rotation of two complex numbers
     __device__ __forceinline__ void rot(R c, R s, C& x, C& y) const {
         const int ns = -s;
-        const C nx{rnd(mad(s, y.re, mad(c, x.re, bias))), rnd(mad(s, y.im, mad(c, x.im, bias)))};
-        const C ny{rnd(mad(c, y.re, mad(ns, x.re, bias))), rnd(mad(c, y.im, mad(ns, x.im, bias)))};
+        const C nx{rnd(mad(s, y.re, mul(c, x.re))), rnd(mad(s, y.im, mul(c, x.im)))};
+        const C ny{rnd(mad(c, y.re, mul(ns, x.re))), rnd(mad(c, y.im, mul(ns, x.im)))};
         x = nx;
         y = ny;
     }
     // |z|^2 exactly, as Q2.60 in 64 bits
-    static __device__ __forceinline__ long long norm2(C z) { return mad(z.im, z.im, mad(z.re, z.re, 0LL)); }
+    static __device__ __forceinline__ long long norm2(C z) { return mad(z.im, z.im, mul(z.re, z.re)); }
     // Q2.60 probability -> float, one rounding; the completed entries of the
     // doubly stochastic matrix may come out a few 1e-10 below zero: clamp
     static __device__ __forceinline__ float to_prob(long long q) {

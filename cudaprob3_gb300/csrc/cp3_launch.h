@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <string>
 
 #include "cp3_internal.h"
 
@@ -24,7 +25,6 @@ struct PropArgs {
     const void* len;
     const int* maxl;
     const int4* ptab;  // mixed: 257 (Q1.30 cos, Q1.30 sin, float cos, float sin) of 2*pi*j/256
-    long long bias;    // 1 << 29, the rounding constant of the Q1.30 path
     void* out;
     int n_cos, n_en, n_en_pad, nl, nl_pad, cchunk;
     double c23, s23, cd, sd;     // FP64 flavour rotation
@@ -38,6 +38,9 @@ inline int propagate_max_threads(bool mixed) { return mixed ? 256 : 128; }
 cudaError_t launch_prep(bool mixed, PrepArgs a, cudaStream_t s);
 cudaError_t launch_propagate(bool mixed, const PropArgs& a, int te, int groups, size_t smem,
                              cudaStream_t s);
+
+// Message returned by cp3_last_error() on this thread.
+void set_last_error(const std::string& msg);
 
 // Throughput of one pipe on the current device (0 mad.wide.s32, 1 FFMA, 2 DFMA).
 cudaError_t measure_pipe(int pipe, double* ops_per_second);

@@ -1,0 +1,267 @@
+// Per-tile and per-thread device code shared by the single-grid kernels
+// (cp3_kernels.cu) and the batched persistent kernel (cp3_batch.cu).
+//
+//   prep_energy_layer  FP64 eigen-solve of one (energy, layer) and the
+//                      mixed/FP64 table entries derived from it
+//   prep_cosine        segment lengths of one trajectory
+//   process_tile       one block's tile: TE energies x a chunk of cosines of
+//                      one grid -> 9 probability planes
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <type_traits>
+
+#include "cp3_chain.cuh"
+#include "cp3_internal.h"
+#include "cp3_physics.cuh"
+
+namespace cp3 {
+
+// Tables of one grid as the prep kernels write them (see cp3_kernels.cu).
+struct GridTables {
+    void* tab;  // tile-major [n_en_pad/TE][nl][W][TE]
+    void* pe;   // [18][n_en_pad]
+    void* len;  // [n_cos][nl_pad]
+    int n_en_pad, te, nl, nl_pad;
+};
+
+// Thread (l, e) of the energy part: eigen-solve of layer l at energy E, writes
+// kappa (and Lambda'/Gamma' for l = 0, 1), leaves the eigenvectors in `vme`
+// (shared memory) for the overlap pass.
+template <bool MIXED>
+__device__ __forceinline__ void prep_energy_layer(const OscParams& osc, double E, double rhoye, int l, int e,
+                                                  const GridTables& g, double* vme) {
+    const int te = g.te, tile = e / te, lane = e % te;
+    const int W = MIXED ? kMixedWords : kFp64Words;
+    double m[3], V[9];
+    layer_eigen(osc, E, rhoye, m, V);
+    for (int w = 0; w < 9; w++) vme[w] = V[w];
+    const double k1 = phase_turns_per_km(m[1], m[0], E);
+    const double k2 = phase_turns_per_km(m[2], m[0], E);
+    const size_t base = ((size_t)tile * g.nl + l) * W * te + lane;
+    if (MIXED) {
+        int* t = (int*)g.tab;
+        const float k1h = (float)k1, k2h = (float)k2;
+        t[base + 9 * (size_t)te] = __float_as_int(k1h);
+        t[base + 10 * (size_t)te] = __float_as_int((float)(k1 - (double)k1h));
+        t[base + 11 * (size_t)te] = __float_as_int(k2h);
+        t[base + 12 * (size_t)te] = __float_as_int((float)(k2 - (double)k2h));
+    } else {
+        double* t = (double*)g.tab;
+        t[base + 9 * (size_t)te] = k1;
+        t[base + 10 * (size_t)te] = k2;
+    }
+    if (l <= 1) {
+        // per energy: Gamma' = columns e, mu of V_0^T W^dagger (l = 0) and
+        // Lambda' = rows e, mu of W V_1 (l = 1), W = R23 diag(1, 1, e^{i dcp})
+        const double sg = (l == 0) ? -1.0 : 1.0;  // e^{-i dcp} for Gamma', e^{+i dcp} for Lambda'
+        double w[9];
+        for (int k = 0; k < 3; k++) {
+            w[k] = V[k];
+            w[3 + 2 * k] = osc.c23 * V[3 + k] + osc.s23 * osc.cd * V[6 + k];
+            w[4 + 2 * k] = sg * osc.s23 * osc.sd * V[6 + k];
+        }
+        const int off = (l == 0) ? 9 : 0;
+        for (int q = 0; q < 9; q++) {
+            const size_t idx = (size_t)(off + q) * g.n_en_pad + e;
+            if (MIXED)
+                ((int*)g.pe)[idx] = __double2int_rn(w[q] * 1073741824.0);
+            else
+                ((double*)g.pe)[idx] = w[q];
+        }
+    }
+}
+
+// Overlap pass of thread (l, e): T_l = V_{l+1}^T V_l from shared memory; the
+// innermost layer has no successor and keeps the identity.
+template <bool MIXED>
+__device__ __forceinline__ void prep_overlap(int l, int e, const GridTables& g, const double* vme) {
+    const int te = g.te, tile = e / te, lane = e % te;
+    const int W = MIXED ? kMixedWords : kFp64Words;
+    const size_t base = ((size_t)tile * g.nl + l) * W * te + lane;
+    const double* vn = vme + 9;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            const double tij = (l + 1 < g.nl) ? vn[i] * vme[j] + vn[3 + i] * vme[3 + j] + vn[6 + i] * vme[6 + j]
+                                              : (i == j ? 1.0 : 0.0);
+            if (MIXED)
+                ((int*)g.tab)[base + (size_t)(3 * i + j) * te] = __double2int_rn(tij * 1073741824.0);
+            else
+                ((double*)g.tab)[base + (size_t)(3 * i + j) * te] = tij;
+        }
+}
+
+// Segment lengths of trajectory c (layers 0..M, zero beyond).
+template <bool MIXED>
+__device__ __forceinline__ void prep_cosine(double cz, int M, const double* radii, double height_cm, int c,
+                                            const GridTables& g) {
+    const double path = path_length_cm(cz, height_cm);
+    for (int l = 0; l < g.nl_pad; l++) {
+        const double L = (l <= M) ? layer_length_km(radii, l, M, cz, path) : 0.0;
+        const size_t idx = (size_t)c * g.nl_pad + l;
+        if (MIXED) {
+            const float h = (float)L;
+            ((float2*)g.len)[idx] = make_float2(h, (float)(L - (double)h));
+        } else {
+            ((double*)g.len)[idx] = L;
+        }
+    }
+}
+
+// ------------------------------------------------------------ propagate ----
+template <int TE>
+struct MixedSrc {
+    const int* tab;    // shared: [nl][13][TE], offset by the thread's lane
+    const int* pe;     // shared: [18][TE], offset by lane
+    const float2* len; // shared: this cosine's [nl_pad]
+    const int4* ptab;  // shared: 257 (Q1.30 cos, sin, float cos, sin)
+    __device__ __forceinline__ int T(int l, int i, int j) const { return tab[(l * kMixedWords + 3 * i + j) * TE]; }
+    __device__ __forceinline__ int La(int j) const { return pe[j * TE]; }
+    __device__ __forceinline__ Q30::C Lb(int j) const { return Q30::C{pe[(3 + 2 * j) * TE], pe[(4 + 2 * j) * TE]}; }
+    __device__ __forceinline__ int Ga(int k) const { return pe[(9 + k) * TE]; }
+    __device__ __forceinline__ Q30::C Gb(int k) const { return Q30::C{pe[(12 + 2 * k) * TE], pe[(13 + 2 * k) * TE]}; }
+    __device__ __forceinline__ void phase(int l, int& c1, int& s1, int& n1, int& c2, int& s2, int& n2) const {
+        const float2 L = len[l];
+        const int* k = tab + (l * kMixedWords + 9) * TE;
+        phase_q30(__int_as_float(k[0]), __int_as_float(k[TE]), L.x, L.y, ptab, c1, s1);
+        phase_q30(__int_as_float(k[2 * TE]), __int_as_float(k[3 * TE]), L.x, L.y, ptab, c2, s2);
+        n1 = -s1;
+        n2 = -s2;
+    }
+};
+
+template <int TE>
+struct F64Src {
+    const double* tab;  // shared: [nl][11][TE], offset by lane
+    const double* pe;
+    const double* len;
+    __device__ __forceinline__ double T(int l, int i, int j) const { return tab[(l * kFp64Words + 3 * i + j) * TE]; }
+    __device__ __forceinline__ double La(int j) const { return pe[j * TE]; }
+    __device__ __forceinline__ F64::C Lb(int j) const { return F64::C{pe[(3 + 2 * j) * TE], pe[(4 + 2 * j) * TE]}; }
+    __device__ __forceinline__ double Ga(int k) const { return pe[(9 + k) * TE]; }
+    __device__ __forceinline__ F64::C Gb(int k) const { return F64::C{pe[(12 + 2 * k) * TE], pe[(13 + 2 * k) * TE]}; }
+    __device__ __forceinline__ void phase(int l, double& c1, double& s1, double& n1, double& c2, double& s2,
+                                          double& n2) const {
+        const double L = len[l];
+        const double* k = tab + (l * kFp64Words + 9) * TE;
+        phase_f64(k[0], L, c1, s1);
+        phase_f64(k[TE], L, c2, s2);
+        n1 = -s1;
+        n2 = -s2;
+    }
+};
+
+// Copy `n16` 16-byte units from global to shared with the whole block.
+__device__ __forceinline__ void block_copy16(void* dst, const void* src, int n16) {
+    const int nt = blockDim.x * blockDim.y, t = threadIdx.y * blockDim.x + threadIdx.x;
+    int4* d = (int4*)dst;
+    const int4* s = (const int4*)src;
+    for (int i = t; i < n16; i += nt) d[i] = __ldg(s + i);
+}
+
+
+// Shared-memory layout of one tile (bytes); `cchunk` bounds the cosine chunk.
+struct TileSmem {
+    size_t tab, pe, ptab, len, maxl, total;
+};
+__host__ __device__ inline TileSmem tile_smem(bool mixed, int te, int nl, int nl_pad, int cchunk) {
+    const size_t word = mixed ? 4 : 8;
+    const size_t W = mixed ? kMixedWords : kFp64Words;
+    TileSmem t;
+    t.tab = 0;
+    t.pe = t.tab + (size_t)nl * W * te * word;
+    t.ptab = t.pe + (size_t)kPerEWords * te * word;
+    t.len = t.ptab + (mixed ? kPhaseTabBytes : 0);
+    t.maxl = t.len + (size_t)cchunk * nl_pad * 8;
+    t.total = (t.maxl + (size_t)cchunk * 4 + 15) / 16 * 16;
+    return t;
+}
+
+// One tile of one grid: energies [etile*TE, etile*TE + TE) and cosines
+// [c0, c0 + ncl).  The block stages the tile's tables in shared memory and
+// each (lane, group) thread walks its cosines.  The phase table must already
+// be in shared memory (stage_phase_table).  Callers synchronise the block
+// between consecutive tiles.
+struct TileJob {
+    const void* tab;   // grid's tile-major table
+    const void* pe;    // grid's [18][n_en_pad]
+    const void* len;   // grid's [n_cos][nl_pad]
+    const int* maxl;   // grid's layer counts
+    void* out;         // grid's [9][n_cos][n_en]
+    int n_cos, n_en, n_en_pad;
+    int etile, c0, ncl;
+};
+
+template <bool MIXED>
+__device__ __forceinline__ void stage_phase_table(unsigned char* smem, const TileSmem& L, const int4* ptab) {
+    if (!MIXED) return;
+    const int nt = blockDim.x * blockDim.y, t = threadIdx.y * blockDim.x + threadIdx.x;
+    int4* s = (int4*)(smem + L.ptab);
+    for (int i = t; i < kPhaseTabN + 1; i += nt) s[i] = ptab[i];
+}
+
+template <bool MIXED, int TE>
+__device__ __forceinline__ void process_tile(const TileJob& j, int nl, int nl_pad, unsigned char* smem,
+                                             const TileSmem& L) {
+    using Word = typename std::conditional<MIXED, int, double>::type;
+    constexpr int W = MIXED ? kMixedWords : kFp64Words;
+    Word* s_tab = (Word*)(smem + L.tab);
+    Word* s_pe = (Word*)(smem + L.pe);
+    const int4* s_ptab = (const int4*)(smem + L.ptab);
+    unsigned char* s_len_raw = smem + L.len;
+    int* s_maxl = (int*)(smem + L.maxl);
+    const size_t tab_words = (size_t)nl * W * TE;
+    block_copy16(s_tab, (const Word*)j.tab + (size_t)j.etile * tab_words, (int)(tab_words * sizeof(Word) / 16));
+    {
+        const int nt = blockDim.x * blockDim.y, t = threadIdx.y * blockDim.x + threadIdx.x;
+        const Word* pe = (const Word*)j.pe;
+        for (int i = t; i < kPerEWords * TE; i += nt) {
+            const int w = i / TE, lane = i % TE;
+            s_pe[i] = pe[(size_t)w * j.n_en_pad + (size_t)j.etile * TE + lane];
+        }
+        const int nlen16 = j.ncl * nl_pad / 2;  // 8-byte entries, nl_pad even
+        block_copy16(s_len_raw, (const unsigned char*)j.len + (size_t)j.c0 * nl_pad * 8, nlen16);
+        for (int i = t; i < j.ncl; i += nt) s_maxl[i] = j.maxl[j.c0 + i];
+    }
+    __syncthreads();
+
+    const int lane = threadIdx.x;
+    const int e = j.etile * TE + lane;
+    const bool store = e < j.n_en;
+    const size_t plane = (size_t)j.n_cos * j.n_en;
+    for (int cl = threadIdx.y; cl < j.ncl; cl += blockDim.y) {
+        const int M = s_maxl[cl];
+        const int ci = j.c0 + cl;
+        if (MIXED) {
+            MixedSrc<TE> src{(const int*)s_tab + lane, (const int*)s_pe + lane,
+                             (const float2*)s_len_raw + (size_t)cl * nl_pad, s_ptab};
+            const Q30 ar{};
+            Q30::C B[4];
+            flavour_block<Q30>(ar, src, M, B);
+            float pr[9];
+            Q30::complete(B, pr);
+            if (store) {
+                float* out = (float*)j.out + (size_t)ci * j.n_en + e;
+#pragma unroll
+                for (int t = 0; t < 9; t++) __stcs(out + (size_t)t * plane, pr[t]);
+            }
+        } else {
+            F64Src<TE> src{(const double*)s_tab + lane, (const double*)s_pe + lane,
+                           (const double*)s_len_raw + (size_t)cl * nl_pad};
+            const F64 ar{};
+            F64::C B[4];
+            flavour_block<F64>(ar, src, M, B);
+            double pr[9];
+            F64::complete(B, pr);
+            if (store) {
+                double* out = (double*)j.out + (size_t)ci * j.n_en + e;
+#pragma unroll
+                for (int t = 0; t < 9; t++) __stcs(out + (size_t)t * plane, pr[t]);
+            }
+        }
+    }
+}
+
+}  // namespace cp3

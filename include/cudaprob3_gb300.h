@@ -154,6 +154,49 @@ int cp3_last_kernel_ms(cp3_propagator* p, float* prep_ms, float* propagate_ms);
 #define CP3_PIPE_DFMA 2
 int cp3_pipe_peak(int device, int pipe, double* ops_per_second);
 
+/* ------------------------------------------------------------------ batches
+ * Many independent propagations ("parameter sets") evaluated together: set s
+ * has its own oscillation parameters, density scale and grid of
+ * n_cosines[s] x n_energies[s] pairs, and its results are the reference's
+ * [9][n_cosines[s]][n_energies[s]] planes at element offset offsets[s].  One
+ * calculation is one CUDA-graph launch: a counter reset, one FP64 precompute
+ * kernel over all sets and one persistent kernel that takes (set, energy
+ * tile, cosine chunk) work items, largest first.  No reference counterpart
+ * (the reference evaluates one parameter point per calculateProbabilities).
+ * Errors are reported through cp3_last_error() like the single-grid ABI. */
+typedef struct cp3_batch cp3_batch;
+
+int cp3_batch_create(cp3_batch** out, int device_id, int precision, int n_sets,
+                     const int* n_cosines, const int* n_energies);
+int cp3_batch_destroy(cp3_batch* b);
+/* all sets' cosines, then all sets' energies, concatenated in set order */
+int cp3_batch_set_grids(cp3_batch* b, const double* cosines, const double* energies);
+/* params[6*s + k]: theta12, theta13, theta23, dcp (rad), dm12sq, dm23sq (eV^2) */
+int cp3_batch_set_parameters(cp3_batch* b, const double* params);
+/* one body for all sets; densities of set s multiplied by scale[s] (NULL: 1) */
+int cp3_batch_set_density(cp3_batch* b, const double* radii, const double* rhos,
+                          const double* ye, int n, const double* scale);
+int cp3_batch_set_production_height(cp3_batch* b, double height_km);
+int cp3_batch_set_stream(cp3_batch* b, void* cuda_stream);
+/* energies per tile (32, 64, 128), cosine groups per block, cosines per item */
+int cp3_batch_set_launch_shape(cp3_batch* b, int te, int groups, int cchunk);
+int cp3_batch_get_launch_shape(cp3_batch* b, int* te, int* groups, int* cchunk, int* blocks);
+/* times every supported launch shape on `reps` launches and keeps the fastest */
+int cp3_batch_autotune(cp3_batch* b, int type, int reps, int* te, int* groups, int* cchunk,
+                       float* best_ms);
+int cp3_batch_calculate(cp3_batch* b, int type);
+int cp3_batch_calculate_async(cp3_batch* b, int type);
+int cp3_batch_wait(cp3_batch* b);
+/* the same work as two single-grid launches per set (for comparison) */
+int cp3_batch_calculate_sequential(cp3_batch* b, int type);
+/* device time of the last calculation (events around the graph or launches) */
+int cp3_batch_last_ms(cp3_batch* b, float* ms);
+/* n_sets + 1 element offsets of each set's planes in the result buffer */
+int cp3_batch_result_offsets(cp3_batch* b, long long* offsets);
+int cp3_batch_result_device_ptr(cp3_batch* b, void** dptr);
+int cp3_batch_copy_results_to_host(cp3_batch* b, void* dst, size_t bytes);
+int cp3_batch_get_maxlayers(cp3_batch* b, int* out, long long n);
+
 #ifdef __cplusplus
 }
 #endif
