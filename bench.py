@@ -49,6 +49,10 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="target CPU time of the baseline sample")
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--workload", choices=["grid4096", "batch", "precision", "gradient"], default="grid4096",
+                    help="grid4096: the headline line; batch: 1024 parameter sets with uneven grids in one "
+                         "graph launch; precision: 64 parameter sets on the 8192 x 8192 grid")
+    ap.add_argument("--sets", type=int, default=0, help="number of parameter sets (batch/precision)")
     return ap.parse_args()
 
 
@@ -407,12 +411,234 @@ def run_ours(args, world, rank, local):
         p.close()
 
 
+# ------------------------------------------------------------ batch sets --
+BATCH_SEED = 3
+
+
+def batch_sets(n):
+    """The batched workload: n parameter sets drawn around the nominal point
+    (seed 0, as the precision workload), each with its own grid: cosine count
+    uniform-integer 64..1024 over [-1, 0], energy count uniform-integer
+    64..2048 log-spaced over 0.5-100 GeV, densities scaled by U(0.97, 1.03)
+    (grid sizes and scales from seed 3)."""
+    from cudaprob3_gb300 import grids as G
+    rng = np.random.default_rng(BATCH_SEED)
+    nc = rng.integers(64, 1025, size=n)
+    ne = rng.integers(64, 2049, size=n)
+    scale = rng.uniform(0.97, 1.03, size=n)
+    params = G.draw_parameter_sets(n, seed=0)
+    cos = [G.linspace(-1.0, 0.0, int(c)) for c in nc]
+    en = [G.logspace(0.5, 100.0, int(e)) for e in ne]
+    return nc, ne, params, scale, cos, en
+
+
+def run_batch(args, world, rank, local):
+    import torch
+
+    from cudaprob3_gb300 import grids as G
+    from cudaprob3_gb300.batch import BatchPropagator
+    import oracle
+
+    torch.cuda.set_device(local)
+    n = args.sets or 1024
+    nc, ne, params, scale, cos, en = batch_sets(n)
+    B = G.PREM_12
+    b = BatchPropagator(local, nc, ne, precision="mixed")
+    b.set_grids(cos, en)
+    b.set_parameters(params)
+    b.set_density(B.radii, B.rhos, B.ye, scale)
+    b.set_production_height(22.0)
+    t0 = time.perf_counter()
+    shape, tune_ms = b.autotune(0, reps=1)
+    tune_s = time.perf_counter() - t0
+    pairs = b.total_pairs
+    for _ in range(args.warmup):
+        b.calculate(0)
+    barrier(world)
+    times = []
+    for k in range(args.steps):
+        b.calculate(k % 2)
+        times.append(b.last_ms())
+    ms = allmax(world, float(np.mean(times)))
+    seq = []
+    for k in range(max(1, min(args.steps, 5))):
+        b.calculate_sequential(k % 2)
+        seq.append(b.last_ms())
+    seq_ms = allmax(world, float(np.mean(seq)))
+    # parity of a few sets against the oracle (strided subsets)
+    b.calculate(0)
+    flat = b.results()
+    err = 0.0
+    for s_ in range(0, n, max(1, n // 8)):
+        got = b.set_result(flat, s_)
+        ic = np.arange(0, nc[s_], 16)
+        ie = np.arange(0, ne[s_], 16)
+        want = oracle.calculate(cos[s_][ic], en[s_][ie], B.radii, B.rho_eff() * scale[s_], tuple(params[s_]),
+                                22.0, False)
+        err = max(err, float(np.abs(got[:, ic][:, :, ie].astype(np.float64) - want).max()))
+    te, groups, cchunk, blocks = b.launch_shape()
+    if rank == 0:
+        line = {"metric": "(cos,E) pairs/s, %d parameter sets with uneven grids in one persistent CUDA-graph "
+                          "launch (mixed)" % n,
+                "value": world * pairs / (ms * 1e-3), "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "i32 Q1.30 chain + f32 phases + f64 eigen-solve (float out)",
+                "data": "synthetic",
+                "config": {"workload": "%d sets, cosines U{64..1024} in [-1,0], energies U{64..2048} over "
+                                       "0.5-100 GeV, density scale U(0.97,1.03), seeds 0 (parameters) and 3 "
+                                       "(grids)" % n, "pairs_per_step": pairs,
+                           "l2": "outputs %.1f GB per step exceed L2" % (pairs * 36 / 1e9),
+                           "launch_shape": {"te": te, "groups": groups, "cchunk": cchunk, "blocks": blocks},
+                           "autotune_s": tune_s, "autotune_best_ms": tune_ms},
+                "sequential": {"value": world * pairs / (seq_ms * 1e-3), "unit": "pairs/s", "ms_per_step": seq_ms,
+                               "launches_per_step": 2 * n},
+                "speedup_vs_sequential": seq_ms / ms, "gpu_launches": 1 + 2 * args.steps,
+                "precision": {"max_abs_dp_vs_oracle_sampled_sets": err}}
+        print(json.dumps(line), flush=True)
+    b.close()
+
+
+def run_precision(args, world, rank, local):
+    import torch
+
+    import cudaprob3_gb300 as cp
+    from cudaprob3_gb300 import grids as G
+    import oracle
+
+    torch.cuda.set_device(local)
+    n = 8192
+    nsets = args.sets or 64
+    cos = G.linspace(-1.0, 0.0, n)
+    en = G.logspace(0.1, 1000.0, n)
+    B = G.PREM_12
+    sets = G.draw_parameter_sets(nsets, seed=0)
+    pm = make_prop(cp, "mixed", cos, en, B, G.NOMINAL, local)
+    pf = make_prop(cp, "fp64", cos, en, B, G.NOMINAL, local)
+    bm = torch.empty((9, n, n), dtype=torch.float32, device=local)
+    bf = torch.empty((9, n, n), dtype=torch.float64, device=local)
+    pm.set_result_buffer(bm.data_ptr(), bm.numel() * 4)
+    pf.set_result_buffer(bf.data_ptr(), bf.numel() * 8)
+    stream = torch.cuda.Stream(device=local)
+    pm.set_stream(stream.cuda_stream)
+    pf.set_stream(stream.cuda_stream)
+    idx = np.arange(0, n, 128)
+    per_set = []
+    tm = []
+    tf = []
+    for k, ps in enumerate(sets):
+        anti = bool(k % 2)
+        t = cp.Antineutrino if anti else cp.Neutrino
+        for p in (pm, pf):
+            p.setMNSMatrix(*ps[:4])
+            p.setNeutrinoMasses(*ps[4:])
+        with torch.cuda.stream(stream):
+            for p, acc in ((pm, tm), (pf, tf)):
+                a = torch.cuda.Event(enable_timing=True)
+                c = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                p.calculateProbabilitiesAsync(t)
+                c.record(stream)
+                c.synchronize()
+                acc.append(a.elapsed_time(c))
+            d = (bm.double() - bf).abs()
+            dmax, dmean = float(d.max()), float(d.mean())
+            del d
+        want = oracle.calculate(cos[idx], en[idx], B.radii, B.rho_eff(), tuple(ps), 22.0, anti)
+        gm = bm[:, idx][:, :, idx].double().cpu().numpy()
+        gf = bf[:, idx][:, :, idx].cpu().numpy()
+        per_set.append({"set": k, "anti": anti, "max_vs_fp64": dmax, "mean_vs_fp64": dmean,
+                        "max_mixed_vs_oracle": float(np.abs(gm - want).max()),
+                        "max_fp64_vs_oracle": float(np.abs(gf - want).max())})
+    pairs = n * n
+    mix_ms = float(np.median(tm))
+    f64_ms = float(np.median(tf))
+    if rank == 0:
+        line = {"metric": "per-set max/mean |dP| of the mixed kernel, 8192 x 8192, %d parameter sets" % nsets,
+                "value": max(r["max_vs_fp64"] for r in per_set), "unit": "max |dP| mixed vs FP64 (all pairs)",
+                "higher_is_better": False, "n_gpus": world, "data": "synthetic",
+                "config": {"workload": "8192 cos x 8192 E (0.1-1000 GeV), 11-shell PREM, %d sets from seed 0 "
+                                       "(nu for even sets, nubar for odd)" % nsets,
+                           "oracle_subset": "every 128th cosine and energy (64 x 64) per set"},
+                "mixed_pairs_per_s": pairs / (mix_ms * 1e-3), "fp64_pairs_per_s": pairs / (f64_ms * 1e-3),
+                "speedup": f64_ms / mix_ms, "mean_of_means_vs_fp64": float(np.mean([r["mean_vs_fp64"] for r in per_set])),
+                "max_mixed_vs_oracle": max(r["max_mixed_vs_oracle"] for r in per_set),
+                "max_fp64_vs_oracle": max(r["max_fp64_vs_oracle"] for r in per_set),
+                "per_set": per_set}
+        print(json.dumps(line), flush=True)
+    pm.close()
+    pf.close()
+
+
+def run_gradient(args, world, rank, local):
+    """400 x 200 binned Poisson log-likelihood: gradient evaluations/s (FP64
+    and mixed adjoint) and the relative error of each against central finite
+    differences (h = 1e-6 relative) of the FP64 oracle (the checker)."""
+    import torch
+
+    from cudaprob3_gb300.loglik import PARAM_NAMES, binned_problem
+    import oracle
+
+    torch.cuda.set_device(local)
+    prob = binned_problem(device_id=local)
+    B = prob.body
+    x0 = np.concatenate([prob.nominal, B.rhos])
+
+    def oracle_ll(x):
+        p = oracle.calculate(prob.cosines, prob.energies, B.radii, (x[6:] * B.ye) / 0.5, tuple(x[:6]), prob.height,
+                             False)
+        return prob.loglik(p[1], p[4])
+
+    fd = np.zeros_like(x0)
+    for k in range(x0.size):
+        h = 1e-6 * abs(x0[k])
+        xp, xm = x0.copy(), x0.copy()
+        xp[k] += h
+        xm[k] -= h
+        fd[k] = (oracle_ll(xp) - oracle_ll(xm)) / (2 * h)
+    out = {}
+    for precision in ("fp64", "mixed"):
+        L = prob.make(device_id=local, precision=precision)
+        for _ in range(max(3, args.warmup)):
+            ll, g = L.evaluate(prob.nominal, B.rhos)
+        n = max(20, args.steps)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(n):
+            ll, g = L.evaluate(prob.nominal, B.rhos)
+        dt = (time.perf_counter() - t0) / n
+        rel = np.abs(g - fd) / np.linalg.norm(fd)
+        out[precision] = {"evals_per_s": 1.0 / dt, "ms_per_eval": dt * 1e3, "loglik": ll,
+                          "max_rel_grad_error": float(rel.max()),
+                          "rel_grad_error_per_param": {n_: float(r) for n_, r in
+                                                       zip(list(PARAM_NAMES) + ["rho_row%d" % i for i in range(B.rhos.size)],
+                                                           rel)},
+                          "gradient": g.tolist()}
+        L.close()
+    if rank == 0:
+        line = {"metric": "gradient evaluations/s, binned Poisson log-likelihood 400 cos x 200 E (adjoint)",
+                "value": out["mixed"]["evals_per_s"], "unit": "evaluations/s", "higher_is_better": True,
+                "n_gpus": world, "data": "synthetic",
+                "config": {"workload": "400 x 200 bins (cos [-1,0], 0.5-100 GeV log), flux E^-2.7 (nu_e = nu_mu/2), "
+                                       "1e6 expected events, Poisson counts seed 1 at nominal + 1 sigma "
+                                       "(theta23, dcp, dm32); gradient w.r.t. 6 parameters + 12 row densities",
+                           "wall_clock": "one evaluate() = graph launch with parameter upload and gradient "
+                                         "download, host-timed"},
+                "fp64": out["fp64"], "mixed": out["mixed"], "finite_differences": fd.tolist()}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_init(args)
     try:
         if args.impl == "reference":
             run_reference(args, world, rank)
+        elif args.workload == "batch":
+            run_batch(args, world, rank, local)
+        elif args.workload == "precision":
+            run_precision(args, world, rank, local)
+        elif args.workload == "gradient":
+            run_gradient(args, world, rank, local)
         else:
             run_ours(args, world, rank, local)
     finally:

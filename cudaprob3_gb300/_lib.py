@@ -74,6 +74,14 @@ SIGNATURES = [
     ("cp3_batch_result_device_ptr", _I, [_P, ctypes.POINTER(_P)]),
     ("cp3_batch_copy_results_to_host", _I, [_P, _P, _SZ]),
     ("cp3_batch_get_maxlayers", _I, [_P, _IP, ctypes.c_longlong]),
+    ("cp3_loglik_create", _I, [ctypes.POINTER(_P), _I, _I, _I, _I]),
+    ("cp3_loglik_destroy", _I, [_P]),
+    ("cp3_loglik_set_bins", _I, [_P, _DP, _DP]),
+    ("cp3_loglik_set_body", _I, [_P, _DP, _DP, _I]),
+    ("cp3_loglik_set_production_height", _I, [_P, _D]),
+    ("cp3_loglik_set_flux", _I, [_P, _DP, _DP, _D]),
+    ("cp3_loglik_set_observed", _I, [_P, _DP]),
+    ("cp3_loglik_evaluate", _I, [_P, _I, _DP, _DP, _DP, _DP]),
 ]
 
 PIPE_IMAD_WIDE = 0

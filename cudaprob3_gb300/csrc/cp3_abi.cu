@@ -384,6 +384,7 @@ int cp3_calculate_probabilities_async(cp3_propagator* p, int type) {
     if (p->n_cos == 0 || p->n_en == 0) return CP3_OK;
     DeviceGuard g(p->device);
     if (g.err != cudaSuccess) return cuda_fail(g.err, "cudaSetDevice");
+    cudaGetLastError();  // a failed earlier call must not be reported by the launch checks below
     cudaError_t e;
     const int n = (int)p->radii.size();
     const int nl = n + 1;
@@ -426,16 +427,17 @@ int cp3_calculate_probabilities_async(cp3_propagator* p, int type) {
     // launch shape: the energy tile must leave room for the layer table
     int te = p->te, groups = p->groups, cchunk = p->cchunk;
     size_t smem = cp3::propagate_smem_bytes(p->mixed, te, nl, nl_pad, cchunk);
-    while (smem > 227 * 1024 && te > 32) {
+    const size_t smem_max = (size_t)cp3::max_dynamic_smem();
+    while (smem > smem_max && te > 32) {
         te /= 2;
         groups = std::min(groups * 2, cp3::propagate_max_threads(p->mixed) / te);
         smem = cp3::propagate_smem_bytes(p->mixed, te, nl, nl_pad, cchunk);
     }
-    while (smem > 227 * 1024 && cchunk > 8) {
+    while (smem > smem_max && cchunk > 8) {
         cchunk /= 2;
         smem = cp3::propagate_smem_bytes(p->mixed, te, nl, nl_pad, cchunk);
     }
-    if (smem > 227 * 1024) return fail(CP3_ERR_LIMIT, "density table too large for one energy tile");
+    if (smem > smem_max) return fail(CP3_ERR_LIMIT, "density table too large for one energy tile");
     const int n_en_pad = (p->n_en + te - 1) / te * te;
     const size_t word = p->mixed ? 4 : 8;
     const size_t W = p->mixed ? cp3::kMixedWords : cp3::kFp64Words;

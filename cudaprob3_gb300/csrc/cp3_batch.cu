@@ -105,8 +105,8 @@ struct BatchPropArgs {
 template <bool MIXED, int TE>
 __global__ void __launch_bounds__(MIXED ? 256 : 128, 3) batch_propagate_kernel(BatchPropArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ int s_item;
     const TileSmem L = tile_smem(MIXED, TE, a.nl, a.nl_pad, a.cchunk);
+    int& s_item = *(int*)(smem + L.total);  // work-item slot after the tile (all shared memory is dynamic)
     stage_phase_table<MIXED>(smem, L, a.ptab);
     const size_t word = MIXED ? 4 : 8;
     const size_t osz = MIXED ? sizeof(float) : sizeof(double);
@@ -139,7 +139,7 @@ static cudaError_t batch_attr() {
     static bool done = false;
     if (done) return cudaSuccess;
     cudaError_t e = cudaFuncSetAttribute(batch_propagate_kernel<MIXED, TE>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem());
     if (e == cudaSuccess) done = true;
     return e;
 }
@@ -368,8 +368,9 @@ int build_layout(cp3_batch* b) {
     if (!b->items.empty() &&
         (e = cudaMemcpy(b->d_items.p, b->items.data(), b->items.size() * sizeof(int4), cudaMemcpyHostToDevice)))
         return bcuda(e, "cudaMemcpy");
-    b->smem = cp3::tile_smem(b->mixed, b->te, b->nl, b->nl_pad, b->cchunk).total;
-    if (b->smem > 227 * 1024) return bfail(CP3_ERR_LIMIT, "batch: tile tables exceed shared memory; lower te or cchunk");
+    b->smem = cp3::tile_smem(b->mixed, b->te, b->nl, b->nl_pad, b->cchunk).total + 16;  // + work-item slot
+    if ((int)b->smem > cp3::max_dynamic_smem())
+        return bfail(CP3_ERR_LIMIT, "batch: tile tables exceed shared memory; lower te or cchunk");
     int bps = 0;
     if ((e = cp3::batch_occupancy(b->mixed, b->te, b->groups, b->smem, &bps)) != cudaSuccess)
         return bcuda(e, "occupancy");
@@ -736,6 +737,7 @@ int cp3_batch_get_launch_shape(cp3_batch* b, int* te, int* groups, int* cchunk, 
 int cp3_batch_calculate_async(cp3_batch* b, int type) {
     if (!b) return bfail(CP3_ERR_ARGUMENT, "null batch handle");
     Guard g(b->device);
+    cudaGetLastError();  // a failed earlier call must not be reported by the checks below
     if (int rc = ready(b, type)) return rc;
     cudaError_t e;
     if ((e = cudaEventRecord(b->ev[0], b->stream))) return bcuda(e, "cudaEventRecord");
@@ -764,6 +766,7 @@ int cp3_batch_calculate(cp3_batch* b, int type) {
 int cp3_batch_calculate_sequential(cp3_batch* b, int type) {
     if (!b) return bfail(CP3_ERR_ARGUMENT, "null batch handle");
     Guard g(b->device);
+    cudaGetLastError();
     if (int rc = ready(b, type)) return rc;
     cudaError_t e;
     if ((e = cudaEventRecord(b->ev[0], b->stream))) return bcuda(e, "cudaEventRecord");

@@ -78,6 +78,16 @@ __global__ void __launch_bounds__(MIXED ? 256 : 128, 3) propagate_kernel(PropArg
 }
 
 // ------------------------------------------------------------- launchers ----
+int max_dynamic_smem() {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || v <= 0) {
+        cudaGetLastError();
+        return 227 * 1024;
+    }
+    return v;
+}
+
 size_t propagate_smem_bytes(bool mixed, int te, int nl, int nl_pad, int cchunk) {
     return tile_smem(mixed, te, nl, nl_pad, cchunk).total;
 }
@@ -104,7 +114,7 @@ static cudaError_t launch_prop_t(const PropArgs& a, int groups, size_t smem, cud
     static bool configured = false;  // one attribute call per instantiation (per process)
     if (!configured) {
         cudaError_t e = cudaFuncSetAttribute(propagate_kernel<MIXED, TE>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem());
         if (e != cudaSuccess) return e;
         configured = true;
     }

@@ -33,6 +33,9 @@ struct PropArgs {
 
 size_t propagate_smem_bytes(bool mixed, int te, int nl, int nl_pad, int cchunk);
 
+// Largest dynamic shared memory a block of the current device may opt in to.
+int max_dynamic_smem();
+
 // Largest block (threads) the propagate kernel of a precision accepts.
 inline int propagate_max_threads(bool mixed) { return mixed ? 256 : 128; }
 cudaError_t launch_prep(bool mixed, PrepArgs a, cudaStream_t s);

@@ -1,0 +1,995 @@
+// Binned Poisson log-likelihood of the propagated probabilities and its
+// gradient by a hand-written adjoint (reverse mode).
+//
+// No reference counterpart: CUDAProb3++ computes probabilities only.  The
+// forward model per bin b = (cosine c, energy E) is
+//   lambda_b = norm * (flux_e(E) P(e -> mu) + flux_mu(E) P(mu -> mu)),
+//   LL = sum_b n_b ln lambda_b - lambda_b   (constant terms dropped),
+// with P from the same propagation as the probability kernels (real eigen-basis,
+// transpose-symmetric layer chain, 2x2 flavour block; cp3_chain.cuh).  The
+// gradient is taken with respect to theta12, theta13, theta23, dCP, dm12sq,
+// dm23sq and the density of every row of the body (caller's row order).
+//
+// Launches of one evaluation (captured in a CUDA graph together with the
+// parameter upload and the result download):
+//   ll_prep_kernel    FP64 tables of every (energy, layer) and segment lengths
+//   ll_pair_kernel    one warp = one energy x 32 cosines; forward chain, LL and
+//                     seeds, then the backward pass that recomputes each layer
+//                     matrix from the tables (no per-layer storage: the chain is
+//                     un-multiplied with T^T and conj(D)); per-(energy, layer)
+//                     adjoints are summed over the warp's cosines with shuffles
+//   ll_reduce_kernel  one thread per energy: sums the warps' partials,
+//                     re-solves every layer's eigen-problem in FP64 and
+//                     back-propagates through it to the parameters; one block
+//                     sums over energies (fixed order: deterministic)
+// Precision: FP64 does every step in double; MIXED runs ll_pair_kernel in
+// FP32 (phases in double-float) with the FP64 tables and FP64 reduction.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/cudaprob3_gb300.h"
+#include "cp3_launch.h"
+#include "cp3_tile.cuh"
+
+namespace cp3 {
+
+constexpr int kLLTile = 32;          // energies per table tile of the likelihood tables
+constexpr int kLLPerE = 19;          // per (warp, energy): Lambda' (9), Gamma' (9), LL
+constexpr int kLLPerL = 11;          // per (warp, energy, layer): T (9), kappa (2)
+constexpr int kLLMaxParams = 6 + kMaxRows;
+
+// ------------------------------------------------------------ complex ----
+template <class T>
+struct Cx {
+    T re, im;
+};
+template <class T>
+__device__ __forceinline__ Cx<T> cx(T r, T i) { return Cx<T>{r, i}; }
+template <class T>
+__device__ __forceinline__ Cx<T> operator+(Cx<T> a, Cx<T> b) { return Cx<T>{a.re + b.re, a.im + b.im}; }
+template <class T>
+__device__ __forceinline__ Cx<T> operator*(Cx<T> a, Cx<T> b) {
+    return Cx<T>{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <class T>
+__device__ __forceinline__ Cx<T> operator*(T t, Cx<T> a) { return Cx<T>{t * a.re, t * a.im}; }
+template <class T>
+__device__ __forceinline__ Cx<T> cj(Cx<T> a) { return Cx<T>{a.re, -a.im}; }
+// conj(a) * b
+template <class T>
+__device__ __forceinline__ Cx<T> cjmul(Cx<T> a, Cx<T> b) {
+    return Cx<T>{a.re * b.re + a.im * b.im, a.re * b.im - a.im * b.re};
+}
+
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// e^{2 pi i t}, t = kappa * L turns; double: exact product and reduction;
+// float: double-float product, exact reduction, then FP32 sincospi.
+__device__ __forceinline__ Cx<double> phase_of(double kappa, double L) {
+    const double t = kappa * L;
+    const double r = t - rint(t);
+    double s, c;
+    sincospi(2.0 * r, &s, &c);
+    return Cx<double>{c, s};
+}
+__device__ __forceinline__ Cx<float> phase_of(float2 kap, float2 L) {
+    const float p = kap.x * L.x;
+    float e = fmaf(kap.x, L.x, -p);
+    e = fmaf(kap.x, L.y, e);
+    e = fmaf(kap.y, L.x, e);
+    const float r = (p - rintf(p)) + e;
+    float s, c;
+    sincospif(2.0f * r, &s, &c);
+    return Cx<float>{c, s};
+}
+
+struct LLArgs {
+    // inputs on the device
+    const OscParams* osc;
+    const double* rhoye;    // [nl]
+    const double* energies; // [n_en]
+    const double* cosines;  // [n_cos]
+    const int* maxl;        // [n_cos]
+    const double* radii;    // [nl-1]
+    const double* flux_e;   // [n_en]
+    const double* flux_mu;  // [n_en]
+    const double* counts;   // [n_cos][n_en]
+    double norm, height_cm;
+    int n_cos, n_en, n_en_pad, nl, nl_pad, n_cchunk;
+    int anti;
+    // tables (FP64, tile kLLTile)
+    double* tab;
+    double* pe;
+    double* len;
+    // partials and results
+    double* part_l;  // [n_cchunk][n_en][nl][11]
+    double* part_e;  // [n_cchunk][n_en][19]
+    double* out;     // [1 + 6 + nrows]: LL, gradient
+    const int* layer_row;  // [nl]: caller's row of layer l (l >= 1), -1 for layer 0
+    int n_rows;
+    const double* ye_layer;  // [nl]
+};
+
+// ---------------------------------------------------------------- prep ----
+__global__ void __launch_bounds__(256) ll_prep_kernel(LLArgs a) {
+    extern __shared__ double s_v[];
+    const int nl = a.nl, eb = blockDim.y;
+    const int nbE = (a.n_en_pad + eb - 1) / eb;
+    const GridTables g{a.tab, a.pe, a.len, a.n_en_pad, kLLTile, nl, a.nl_pad};
+    if ((int)blockIdx.x < nbE) {
+        const int l = threadIdx.x, ey = threadIdx.y;
+        const int e = blockIdx.x * eb + ey;
+        const bool live = (l < nl) && (e < a.n_en_pad);
+        double* vme = s_v + ((size_t)ey * nl + (l < nl ? l : 0)) * 9;
+        if (live) {
+            const double E = a.energies[e < a.n_en ? e : a.n_en - 1];
+            prep_energy_layer<false>(*a.osc, E, a.rhoye[l], l, e, g, vme);
+        }
+        __syncthreads();
+        if (live) prep_overlap<false>(l, e, g, vme);
+    } else {
+        const int c = (blockIdx.x - nbE) * (blockDim.x * blockDim.y) + threadIdx.y * blockDim.x + threadIdx.x;
+        if (c >= a.n_cos) return;
+        prep_cosine<false>(a.cosines[c], a.maxl[c], a.radii, a.height_cm, c, g);
+    }
+}
+
+// ---------------------------------------------------------- pair kernel ----
+// Table accessors for energy e (uniform across the warp).
+struct LLTab {
+    const double* tab;
+    const double* pe;
+    int e, nl, n_en_pad;
+    __device__ __forceinline__ double T(int l, int i, int j) const {
+        const int tile = e / kLLTile, lane = e % kLLTile;
+        return tab[(((size_t)tile * nl + l) * kFp64Words + 3 * i + j) * kLLTile + lane];
+    }
+    __device__ __forceinline__ double kap(int l, int k) const {
+        const int tile = e / kLLTile, lane = e % kLLTile;
+        return tab[(((size_t)tile * nl + l) * kFp64Words + 9 + k) * kLLTile + lane];
+    }
+    __device__ __forceinline__ double pe_w(int w) const { return pe[(size_t)w * n_en_pad + e]; }
+};
+
+template <class R>
+struct Phase;
+template <>
+struct Phase<double> {
+    // e^{i psi_k} of layer l, k = 1, 2 (table words kappa_1, kappa_2)
+    __device__ static Cx<double> get(const LLTab& t, int l, int k, const double* len) {
+        return phase_of(t.kap(l, k - 1), len[l]);
+    }
+};
+template <>
+struct Phase<float> {
+    __device__ static Cx<float> get(const LLTab& t, int l, int k, const double* len) {
+        const double kd = t.kap(l, k - 1), Ld = len[l];
+        const float kh = (float)kd, Lh = (float)Ld;
+        return phase_of(make_float2(kh, (float)(kd - (double)kh)), make_float2(Lh, (float)(Ld - (double)Lh)));
+    }
+};
+
+template <class R>
+__global__ void __launch_bounds__(128) ll_pair_kernel(LLArgs a) {
+    using C = Cx<R>;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int e = blockIdx.x * 4 + warp;
+    const int cchunk = blockIdx.y;
+    const int c = cchunk * 32 + lane;
+    if (e >= a.n_en) return;  // whole warp leaves together
+    const bool valid = c < a.n_cos;
+    const int M = valid ? a.maxl[c] : 0;
+    const int Mw = __reduce_max_sync(0xffffffffu, M);
+    const LLTab tb{a.tab, a.pe, e, a.nl, a.n_en_pad};
+    const double* len = a.len + (size_t)(valid ? c : 0) * a.nl_pad;
+    const R twopi = (R)kTwoPi;
+
+    // per-energy tables: Lambda' (row 0 real, row 1 complex), Gamma' (col 0 real, col 1 complex)
+    R La[3];
+    C Lb[3];
+    R Ga[3];
+    C Gb[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        La[k] = (R)tb.pe_w(k);
+        Lb[k] = C{(R)tb.pe_w(3 + 2 * k), (R)tb.pe_w(4 + 2 * k)};
+        Ga[k] = (R)tb.pe_w(9 + k);
+        Gb[k] = C{(R)tb.pe_w(12 + 2 * k), (R)tb.pe_w(13 + 2 * k)};
+    }
+    auto T = [&](int l, int i, int j) -> R { return (R)tb.T(l, i, j); };
+    auto D = [&](int l, int k) -> C { return Phase<R>::get(tb, l, k, len); };  // k = 1, 2
+
+    // ---------------- forward
+    C D0[3] = {C{1, 0}, D(0, 1), D(0, 2)};
+    C g[3][2];  // D_0 Gamma'
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        g[j][0] = Ga[j] * D0[j];
+        g[j][1] = D0[j] * Gb[j];
+    }
+    C x[3][2];  // T_0 g
+    C Y[3][3];
+    C DM[3] = {C{1, 0}, C{1, 0}, C{1, 0}};
+    C G[3][3];
+    C X[3][2];
+    C B[2][2];
+    if (M >= 1) {
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int b = 0; b < 2; b++) x[i][b] = T(0, i, 0) * g[0][b] + T(0, i, 1) * g[1][b] + T(0, i, 2) * g[2][b];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) Y[i][j] = C{(R)(i == j), 0};
+        if (M >= 2) {
+            const C d1[3] = {C{1, 0}, D(1, 1), D(1, 2)};
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int k = 0; k < 3; k++) Y[i][k] = T(1, i, k) * d1[k];
+            for (int l = 2; l < M; l++) {
+                const C dl[3] = {C{1, 0}, D(l, 1), D(l, 2)};
+                C U[3][3];
+#pragma unroll
+                for (int k = 0; k < 3; k++)
+#pragma unroll
+                    for (int j = 0; j < 3; j++) U[k][j] = dl[k] * Y[k][j];
+#pragma unroll
+                for (int i = 0; i < 3; i++)
+#pragma unroll
+                    for (int j = 0; j < 3; j++) Y[i][j] = T(l, i, 0) * U[0][j] + T(l, i, 1) * U[1][j] + T(l, i, 2) * U[2][j];
+            }
+        }
+        DM[1] = D(M, 1);
+        DM[2] = D(M, 2);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                C s{0, 0};
+#pragma unroll
+                for (int k = 0; k < 3; k++) s = s + Y[k][i] * (DM[k] * Y[k][j]);
+                G[i][j] = s;
+            }
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+#pragma unroll
+            for (int b = 0; b < 2; b++) X[k][b] = G[k][0] * x[0][b] + G[k][1] * x[1][b] + G[k][2] * x[2][b];
+#pragma unroll
+        for (int b = 0; b < 2; b++) {
+            B[0][b] = La[0] * X[0][b] + La[1] * X[1][b] + La[2] * X[2][b];
+            B[1][b] = Lb[0] * X[0][b] + Lb[1] * X[1][b] + Lb[2] * X[2][b];
+        }
+    } else {
+        // block = Gamma'^dagger D_0 Gamma'
+#pragma unroll
+        for (int b = 0; b < 2; b++) {
+            B[0][b] = Ga[0] * g[0][b] + Ga[1] * g[1][b] + Ga[2] * g[2][b];
+            B[1][b] = cjmul(Gb[0], g[0][b]) + cjmul(Gb[1], g[1][b]) + cjmul(Gb[2], g[2][b]);
+        }
+    }
+    // probabilities P(e -> mu) = |S[mu][e]|^2 = |B[1][0]|^2, P(mu -> mu) = |B[1][1]|^2
+    const double pem = (double)B[1][0].re * B[1][0].re + (double)B[1][0].im * B[1][0].im;
+    const double pmm = (double)B[1][1].re * B[1][1].re + (double)B[1][1].im * B[1][1].im;
+    double ll = 0.0;
+    R w_em = 0, w_mm = 0;
+    if (valid) {
+        const double fe = a.flux_e[e], fm = a.flux_mu[e];
+        const double lam = a.norm * (fe * pem + fm * pmm);
+        const double n = a.counts[(size_t)c * a.n_en + e];
+        if (lam > 0.0) {
+            ll = n * log(lam) - lam;
+            const double w = (n / lam - 1.0) * a.norm;
+            w_em = (R)(w * fe);
+            w_mm = (R)(w * fm);
+        } else {
+            ll = -lam;
+        }
+    }
+    // ---------------- backward
+    C gB[2][2] = {{C{0, 0}, C{0, 0}}, {(R)2 * w_em * B[1][0], (R)2 * w_mm * B[1][1]}};
+    C gLb[3], gGb[3];  // adjoints of Lambda' row 1 and Gamma' column 1
+    R gLa[3], gGa[3];
+    C gD0[3];
+    R gT0[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        gLb[k] = C{0, 0};
+        gGb[k] = C{0, 0};
+        gLa[k] = 0;
+        gGa[k] = 0;
+        gD0[k] = C{0, 0};
+#pragma unroll
+        for (int j = 0; j < 3; j++) gT0[k][j] = 0;
+    }
+    C gY[3][3];
+    C gDM[3] = {C{0, 0}, C{0, 0}, C{0, 0}};
+    if (M >= 1) {
+        // B = Lambda' X
+        C gX[3][2];
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+#pragma unroll
+            for (int b = 0; b < 2; b++) gX[k][b] = La[k] * gB[0][b] + cjmul(Lb[k], gB[1][b]);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            gLa[k] = (cjmul(X[k][0], gB[0][0]) + cjmul(X[k][1], gB[0][1])).re;
+            gLb[k] = cjmul(X[k][0], gB[1][0]) + cjmul(X[k][1], gB[1][1]);
+        }
+        // X = G x
+        C gx[3][2];
+        C gG[3][3];
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+#pragma unroll
+            for (int b = 0; b < 2; b++) gx[j][b] = cjmul(G[0][j], gX[0][b]) + cjmul(G[1][j], gX[1][b]) + cjmul(G[2][j], gX[2][b]);
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) gG[k][j] = cjmul(x[j][0], gX[k][0]) + cjmul(x[j][1], gX[k][1]);
+        // x = T_0 g
+        C gg[3][2];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) gT0[i][j] = (cjmul(g[j][0], gx[i][0]) + cjmul(g[j][1], gx[i][1])).re;
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+#pragma unroll
+            for (int b = 0; b < 2; b++) gg[j][b] = T(0, 0, j) * gx[0][b] + T(0, 1, j) * gx[1][b] + T(0, 2, j) * gx[2][b];
+        // g = D_0 Gamma'
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            gD0[j] = (Ga[j] * gg[j][0]) + cjmul(Gb[j], gg[j][1]);
+            gGa[j] = cjmul(D0[j], gg[j][0]).re;
+            gGb[j] = cjmul(D0[j], gg[j][1]);
+        }
+        // G = Y^T D_M Y
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            C sd{0, 0};
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                C s{0, 0};
+#pragma unroll
+                for (int j = 0; j < 3; j++) {
+                    s = s + cjmul(Y[k][j], gG[i][j] + gG[j][i]);
+                    sd = sd + cjmul(Y[k][i] * Y[k][j], gG[i][j]);
+                }
+                gY[k][i] = cjmul(DM[k], s);
+            }
+            gDM[k] = sd;
+        }
+    } else {
+        // B = Gamma'^dagger g, g = D_0 Gamma'
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            // from the left factor: B[0][b] += Ga[j] g[j][b], B[1][b] += conj(Gb[j]) g[j][b]
+            gGa[j] = (cjmul(g[j][0], gB[0][0]) + cjmul(g[j][1], gB[0][1])).re;
+            gGb[j] = cj(cjmul(g[j][0], gB[1][0]) + cjmul(g[j][1], gB[1][1]));
+            C ggj0 = Ga[j] * gB[0][0] + Gb[j] * gB[1][0];
+            C ggj1 = Ga[j] * gB[0][1] + Gb[j] * gB[1][1];
+            gD0[j] = Ga[j] * ggj0 + cjmul(Gb[j], ggj1);
+            gGa[j] += cjmul(D0[j], ggj0).re;
+            gGb[j] = gGb[j] + cjmul(D0[j], ggj1);
+        }
+    }
+
+    // per-(energy, layer) partials: layers Mw .. 1 (descending), then layer 0
+    double* pl = a.part_l + ((size_t)cchunk * a.n_en + e) * a.nl * kLLPerL;
+    for (int l = Mw; l >= 1; l--) {
+        R tT[9];
+        R tk[2] = {0, 0};
+#pragma unroll
+        for (int q = 0; q < 9; q++) tT[q] = 0;
+        if (l == M) {
+            // D_M = diag(1, e^{i psi1}, e^{i psi2}): dLL/dkappa_k = 2 pi L * (-Im(conj(gD) D))
+#pragma unroll
+            for (int k = 1; k < 3; k++) tk[k - 1] = -twopi * (R)len[l] * cjmul(gDM[k], DM[k]).im;
+        } else if (l < M) {
+            // Y_l = T_l U, U = D_l Y_{l-1}; un-multiply: U = T_l^T Y_l, Y_{l-1} = conj(D_l) U
+            const C dl[3] = {C{1, 0}, D(l, 1), D(l, 2)};
+            R t[3][3];
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int j = 0; j < 3; j++) t[i][j] = T(l, i, j);
+            C U[3][3], gU[3][3];
+#pragma unroll
+            for (int k = 0; k < 3; k++)
+#pragma unroll
+                for (int j = 0; j < 3; j++) {
+                    U[k][j] = t[0][k] * Y[0][j] + t[1][k] * Y[1][j] + t[2][k] * Y[2][j];
+                    gU[k][j] = t[0][k] * gY[0][j] + t[1][k] * gY[1][j] + t[2][k] * gY[2][j];
+                }
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int k = 0; k < 3; k++)
+                    tT[3 * i + k] = (cjmul(U[k][0], gY[i][0]) + cjmul(U[k][1], gY[i][1]) + cjmul(U[k][2], gY[i][2])).re;
+            if (l >= 2) {
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    C gd{0, 0};
+#pragma unroll
+                    for (int j = 0; j < 3; j++) {
+                        const C yp = cjmul(dl[k], U[k][j]);  // Y_{l-1}[k][j]
+                        gd = gd + cjmul(yp, gU[k][j]);
+                        Y[k][j] = yp;
+                        gY[k][j] = cjmul(dl[k], gU[k][j]);
+                    }
+                    if (k > 0) tk[k - 1] = -twopi * (R)len[l] * cjmul(gd, dl[k]).im;
+                }
+            } else {
+                // l = 1: Y_1 = T_1 D_1, so U = D_1 and gU holds the adjoint of D_1 on the diagonal
+#pragma unroll
+                for (int k = 1; k < 3; k++) tk[k - 1] = -twopi * (R)len[1] * cjmul(gU[k][k], dl[k]).im;
+            }
+        }
+        // warp reduction of this layer's 11 values (lanes with nothing to add give zeros)
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            const double v = warp_sum((double)tT[q]);
+            if (lane == 0) pl[(size_t)l * kLLPerL + q] = v;
+        }
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            const double v = warp_sum((double)tk[k]);
+            if (lane == 0) pl[(size_t)l * kLLPerL + 9 + k] = v;
+        }
+    }
+    // layers above Mw are never crossed by this warp's cosines
+    if (lane == 0)
+        for (int l = Mw + 1; l < a.nl; l++)
+            for (int q = 0; q < kLLPerL; q++) pl[(size_t)l * kLLPerL + q] = 0.0;
+    // layer 0: T_0 and D_0
+    {
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            const double v = warp_sum((double)gT0[q / 3][q % 3]);
+            if (lane == 0) pl[q] = v;
+        }
+#pragma unroll
+        for (int k = 1; k < 3; k++) {
+            const double v = warp_sum((double)(-twopi * (R)len[0] * cjmul(gD0[k], D0[k]).im));
+            if (lane == 0) pl[9 + k - 1] = v;
+        }
+    }
+    // per energy: Lambda', Gamma', LL
+    double* pe = a.part_e + ((size_t)cchunk * a.n_en + e) * kLLPerE;
+    double vals[kLLPerE];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        vals[k] = (double)gLa[k];
+        vals[3 + 2 * k] = (double)gLb[k].re;
+        vals[4 + 2 * k] = (double)gLb[k].im;
+        vals[9 + k] = (double)gGa[k];
+        vals[12 + 2 * k] = (double)gGb[k].re;
+        vals[13 + 2 * k] = (double)gGb[k].im;
+    }
+    vals[18] = ll;
+#pragma unroll
+    for (int q = 0; q < kLLPerE; q++) {
+        const double v = warp_sum(vals[q]);
+        if (lane == 0) pe[q] = v;
+    }
+}
+
+// ---------------------------------------------------------- reduction ----
+// Thread e: sum of the partials of energy e, FP64 eigen back-propagation to
+// the parameters; then a fixed-order block sum over energies.
+__global__ void __launch_bounds__(256) ll_reduce_kernel(LLArgs a) {
+    __shared__ double s_acc[256];
+    const int np = 6 + a.n_rows;
+    double grad[kLLMaxParams + 1];  // [0] LL, then the gradient
+    for (int q = 0; q <= np; q++) grad[q] = 0.0;
+    const OscParams o = *a.osc;
+    for (int e = threadIdx.x; e < a.n_en; e += blockDim.x) {
+        const double E = a.energies[e];
+        double gT[kMaxRows + 1][9], gK[kMaxRows + 1][2];
+        double gL[18];
+        for (int l = 0; l < a.nl; l++) {
+            for (int q = 0; q < 9; q++) gT[l][q] = 0.0;
+            gK[l][0] = gK[l][1] = 0.0;
+        }
+        for (int q = 0; q < 18; q++) gL[q] = 0.0;
+        double ll = 0.0;
+        for (int cc = 0; cc < a.n_cchunk; cc++) {
+            const double* pl = a.part_l + ((size_t)cc * a.n_en + e) * a.nl * kLLPerL;
+            for (int l = 0; l < a.nl; l++) {
+                for (int q = 0; q < 9; q++) gT[l][q] += pl[l * kLLPerL + q];
+                gK[l][0] += pl[l * kLLPerL + 9];
+                gK[l][1] += pl[l * kLLPerL + 10];
+            }
+            const double* pe = a.part_e + ((size_t)cc * a.n_en + e) * kLLPerE;
+            for (int q = 0; q < 18; q++) gL[q] += pe[q];
+            ll += pe[18];
+        }
+        grad[0] += ll;
+        // recompute every layer's eigen-decomposition and back-propagate
+        const double s23 = o.s23, c23 = o.c23, sd = o.sd, cd = o.cd;
+        double gV[kMaxRows + 1][9];
+        double Vs[kMaxRows + 1][9], ms[kMaxRows + 1][3];
+        for (int l = 0; l < a.nl; l++) {
+            layer_eigen(o, E, a.rhoye[l], ms[l], Vs[l]);
+            for (int q = 0; q < 9; q++) gV[l][q] = 0.0;
+        }
+        // T_l = V_{l+1}^T V_l
+        for (int l = 0; l + 1 < a.nl; l++)
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) {
+                    const double t = gT[l][3 * i + j];
+                    for (int r = 0; r < 3; r++) {
+                        gV[l + 1][3 * r + i] += t * Vs[l][3 * r + j];
+                        gV[l][3 * r + j] += t * Vs[l + 1][3 * r + i];
+                    }
+                }
+        // Lambda' from V_1: row 0 = V_1[0][k]; row 1 = c23 V_1[1][k] + s23 e^{i d} V_1[2][k]
+        double gth23 = 0.0, gdcp = 0.0;
+        for (int k = 0; k < 3; k++) {
+            const double gre = gL[3 + 2 * k], gim = gL[4 + 2 * k];
+            gV[1][k] += gL[k];
+            gV[1][3 + k] += c23 * gre;
+            gV[1][6 + k] += s23 * (gre * cd + gim * sd);
+            const double v1 = Vs[1][3 + k], v2 = Vs[1][6 + k];
+            // d/dtheta23: -s23 v1 + c23 e^{id} v2 ; d/ddcp: i s23 e^{id} v2
+            gth23 += gre * (-s23 * v1 + c23 * cd * v2) + gim * (c23 * sd * v2);
+            gdcp += gre * (-s23 * sd * v2) + gim * (s23 * cd * v2);
+        }
+        // Gamma' from V_0: column 0 = V_0[0][k]; column 1 = c23 V_0[1][k] + s23 e^{-i d} V_0[2][k]
+        for (int k = 0; k < 3; k++) {
+            const double gre = gL[12 + 2 * k], gim = gL[13 + 2 * k];
+            gV[0][k] += gL[9 + k];
+            gV[0][3 + k] += c23 * gre;
+            gV[0][6 + k] += s23 * (gre * cd - gim * sd);
+            const double v1 = Vs[0][3 + k], v2 = Vs[0][6 + k];
+            gth23 += gre * (-s23 * v1 + c23 * cd * v2) + gim * (-c23 * sd * v2);
+            gdcp += gre * (-s23 * sd * v2) + gim * (-s23 * cd * v2);
+        }
+        // eigen back-propagation per layer, then H_l = O diag(0, d1, d2) O^T - fac_l e0 e0^T
+        double gth12 = 0.0, gth13 = 0.0, gd1 = 0.0, gd2 = 0.0;
+        // O and its derivatives from the stored O matrix: O = R13 R12
+        const double* O = o.o;
+        const double c13 = O[8], s13 = O[2];
+        const double c12 = (c13 != 0.0) ? O[0] / c13 : O[4];
+        const double sn12 = -O[3];
+        const double dO12[9] = {-c13 * sn12, c13 * c12, 0.0, -c12, -sn12, 0.0, s13 * sn12, -s13 * c12, 0.0};
+        const double dO13[9] = {-s13 * c12, -s13 * sn12, c13, 0.0, 0.0, 0.0, -c13 * c12, -c13 * sn12, -s13};
+        for (int l = 0; l < a.nl; l++) {
+            const double* V = Vs[l];
+            const double* m = ms[l];
+            // dLL/dm_k from the phase rates kappa_k = -LoE (m_k - m_0) / (2 pi E), k = 1, 2
+            const double f = -kLoEfac / (kTwoPi * E);
+            double gm[3] = {-(gK[l][0] + gK[l][1]) * f, gK[l][0] * f, gK[l][1] * f};
+            // gH = sum_k gm_k v_k v_k^T + sum_{k != j} (v_j . gv_k) / (m_k - m_j) v_j v_k^T
+            double W[3][3];  // W[j][k] = coefficient of v_j v_k^T
+            for (int j = 0; j < 3; j++)
+                for (int k = 0; k < 3; k++) {
+                    if (j == k) {
+                        W[j][k] = gm[k];
+                    } else {
+                        double dot = 0.0;
+                        for (int r = 0; r < 3; r++) dot += V[3 * r + j] * gV[l][3 * r + k];
+                        const double gap = m[k] - m[j];
+                        W[j][k] = (gap != 0.0) ? dot / gap : 0.0;
+                    }
+                }
+            double gH[3][3];
+            for (int p = 0; p < 3; p++)
+                for (int q = 0; q < 3; q++) {
+                    double s = 0.0;
+                    for (int j = 0; j < 3; j++)
+                        for (int k = 0; k < 3; k++) s += W[j][k] * V[3 * p + j] * V[3 * q + k];
+                    gH[p][q] = s;
+                }
+            // symmetric part (H is symmetric)
+            for (int p = 0; p < 3; p++)
+                for (int q = p + 1; q < 3; q++) {
+                    const double s = 0.5 * (gH[p][q] + gH[q][p]);
+                    gH[p][q] = gH[q][p] = s;
+                }
+            // d1, d2: o_1^T gH o_1, o_2^T gH o_2
+            for (int p = 0; p < 3; p++)
+                for (int q = 0; q < 3; q++) {
+                    gd1 += gH[p][q] * O[3 * p + 1] * O[3 * q + 1];
+                    gd2 += gH[p][q] * O[3 * p + 2] * O[3 * q + 2];
+                }
+            // theta12, theta13: 2 tr(gH O D dO^T)
+            const double dd[3] = {0.0, o.d1, o.d2};
+            for (int p = 0; p < 3; p++)
+                for (int q = 0; q < 3; q++)
+                    for (int k = 1; k < 3; k++) {
+                        gth12 += 2.0 * gH[p][q] * O[3 * p + k] * dd[k] * dO12[3 * q + k];
+                        gth13 += 2.0 * gH[p][q] * O[3 * p + k] * dd[k] * dO13[3 * q + k];
+                    }
+            // densities: H[0][0] -= fac, fac = sgn GF E rho Ye
+            if (l >= 1) {
+                const int row = a.layer_row[l];
+                const double sgn = a.anti ? 1.0 : -1.0;
+                grad[1 + 6 + row] += -gH[0][0] * sgn * kGF * E * a.ye_layer[l];
+            }
+        }
+        grad[1] += gth12;
+        grad[2] += gth13;
+        grad[3] += gth23;
+        grad[4] += gdcp;
+        // d1 = dm12sq, d2 = dm12sq + dm23sq
+        grad[5] += gd1 + gd2;
+        grad[6] += gd2;
+    }
+    // fixed-order block reduction of each output
+    for (int q = 0; q <= np; q++) {
+        s_acc[threadIdx.x] = grad[q];
+        __syncthreads();
+        for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+            if ((int)threadIdx.x < s) s_acc[threadIdx.x] += s_acc[threadIdx.x + s];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) a.out[q] = s_acc[0];
+        __syncthreads();
+    }
+}
+
+}  // namespace cp3
+
+// ======================================================================= host
+namespace {
+
+int lfail(int code, const std::string& m) {
+    cp3::set_last_error(m);
+    return code;
+}
+int lcuda(cudaError_t e, const char* w) { return lfail(CP3_ERR_CUDA, std::string(w) + ": " + cudaGetErrorString(e)); }
+
+struct LGuard {
+    int prev = -1;
+    cudaError_t err = cudaSuccess;
+    explicit LGuard(int d) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != d) err = cudaSetDevice(d);
+    }
+    ~LGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+}  // namespace
+
+struct cp3_loglik {
+    int device = 0;
+    bool mixed = false;
+    int n_cos = 0, n_en = 0;
+    std::vector<double> cosines, energies, flux_e, flux_mu, counts;
+    std::vector<int> maxl;
+    std::vector<double> radii, ye, coslimit;  // outside-in
+    std::vector<int> layer_row;               // caller row of each layer
+    int n_rows = 0;
+    double height_cm = 0, norm = 1;
+    bool has_bins = false, has_body = false, has_flux = false, has_counts = false, has_height = false;
+    bool dirty = true;
+    int nl = 0, nl_pad = 0, n_en_pad = 0, n_cchunk = 0;
+    cudaStream_t stream = nullptr;
+    // device
+    double *d_en = nullptr, *d_cos = nullptr, *d_radii = nullptr, *d_fe = nullptr, *d_fm = nullptr, *d_counts = nullptr;
+    double *d_tab = nullptr, *d_pe = nullptr, *d_len = nullptr, *d_pl = nullptr, *d_pee = nullptr, *d_out = nullptr;
+    double *d_rhoye = nullptr, *d_yel = nullptr;
+    int *d_maxl = nullptr, *d_row = nullptr;
+    cp3::OscParams* d_osc = nullptr;
+    // pinned staging: [OscParams][rhoye nl] up, [out] down
+    unsigned char* h_up = nullptr;
+    double* h_out = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int graph_type = -1;
+};
+
+namespace {
+
+void ll_free(cp3_loglik* L) {
+    if (L->exec) cudaGraphExecDestroy(L->exec);
+    if (L->graph) cudaGraphDestroy(L->graph);
+    L->exec = nullptr;
+    L->graph = nullptr;
+    void* ptrs[] = {L->d_en, L->d_cos, L->d_radii, L->d_fe, L->d_fm, L->d_counts, L->d_tab, L->d_pe, L->d_len,
+                    L->d_pl, L->d_pee, L->d_out, L->d_rhoye, L->d_yel, L->d_maxl, L->d_row, L->d_osc};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    L->d_en = L->d_cos = L->d_radii = L->d_fe = L->d_fm = L->d_counts = nullptr;
+    L->d_tab = L->d_pe = L->d_len = L->d_pl = L->d_pee = L->d_out = L->d_rhoye = L->d_yel = nullptr;
+    L->d_maxl = L->d_row = nullptr;
+    L->d_osc = nullptr;
+}
+
+size_t up_bytes(const cp3_loglik*) { return sizeof(cp3::OscParams) + sizeof(double) * (cp3::kMaxRows + 1); }
+
+template <class T>
+cudaError_t dmalloc_copy(T** d, const T* h, size_t n) {
+    cudaError_t e = cudaMalloc((void**)d, std::max<size_t>(n, 1) * sizeof(T));
+    if (!e && n) e = cudaMemcpy(*d, h, n * sizeof(T), cudaMemcpyHostToDevice);
+    return e;
+}
+
+cp3::LLArgs ll_args(cp3_loglik* L, int type) {
+    cp3::LLArgs a{};
+    a.osc = L->d_osc;
+    a.rhoye = L->d_rhoye;
+    a.energies = L->d_en;
+    a.cosines = L->d_cos;
+    a.maxl = L->d_maxl;
+    a.radii = L->d_radii;
+    a.flux_e = L->d_fe;
+    a.flux_mu = L->d_fm;
+    a.counts = L->d_counts;
+    a.norm = L->norm;
+    a.height_cm = L->height_cm;
+    a.n_cos = L->n_cos;
+    a.n_en = L->n_en;
+    a.n_en_pad = L->n_en_pad;
+    a.nl = L->nl;
+    a.nl_pad = L->nl_pad;
+    a.n_cchunk = L->n_cchunk;
+    a.anti = type == CP3_ANTINEUTRINO;
+    a.tab = L->d_tab;
+    a.pe = L->d_pe;
+    a.len = L->d_len;
+    a.part_l = L->d_pl;
+    a.part_e = L->d_pee;
+    a.out = L->d_out;
+    a.layer_row = L->d_row;
+    a.n_rows = L->n_rows;
+    a.ye_layer = L->d_yel;
+    return a;
+}
+
+// Device buffers and the evaluation graph: upload, prep, pairs, reduce, download.
+int ll_setup(cp3_loglik* L, int type) {
+    ll_free(L);
+    L->nl = L->n_rows + 1;
+    L->nl_pad = (L->nl + 1) / 2 * 2;
+    L->n_en_pad = (L->n_en + cp3::kLLTile - 1) / cp3::kLLTile * cp3::kLLTile;
+    L->n_cchunk = (L->n_cos + 31) / 32;
+    for (int i = 0; i < L->n_cos; i++) {
+        int cnt = 0;
+        for (double lim : L->coslimit) cnt += (L->cosines[i] < lim);
+        L->maxl[i] = cnt;
+    }
+    std::vector<double> yel(L->nl, 0.0);
+    for (int l = 1; l < L->nl; l++) yel[l] = L->ye[l - 1];
+    cudaError_t e;
+    if ((e = dmalloc_copy(&L->d_en, L->energies.data(), L->n_en)) || (e = dmalloc_copy(&L->d_cos, L->cosines.data(), L->n_cos)) ||
+        (e = dmalloc_copy(&L->d_radii, L->radii.data(), L->radii.size())) ||
+        (e = dmalloc_copy(&L->d_fe, L->flux_e.data(), L->n_en)) || (e = dmalloc_copy(&L->d_fm, L->flux_mu.data(), L->n_en)) ||
+        (e = dmalloc_copy(&L->d_counts, L->counts.data(), L->counts.size())) ||
+        (e = dmalloc_copy(&L->d_maxl, L->maxl.data(), L->n_cos)) ||
+        (e = dmalloc_copy(&L->d_row, L->layer_row.data(), L->layer_row.size())) ||
+        (e = dmalloc_copy(&L->d_yel, yel.data(), yel.size())))
+        return lcuda(e, "loglik inputs");
+    const size_t tab = (size_t)L->n_en_pad * L->nl * cp3::kFp64Words, pe = (size_t)cp3::kPerEWords * L->n_en_pad;
+    const size_t len = (size_t)L->n_cos * L->nl_pad;
+    const size_t pl = (size_t)L->n_cchunk * L->n_en * L->nl * cp3::kLLPerL;
+    const size_t pee = (size_t)L->n_cchunk * L->n_en * cp3::kLLPerE;
+    if ((e = cudaMalloc(&L->d_tab, tab * 8)) || (e = cudaMalloc(&L->d_pe, pe * 8)) || (e = cudaMalloc(&L->d_len, len * 8)) ||
+        (e = cudaMalloc(&L->d_pl, pl * 8)) || (e = cudaMalloc(&L->d_pee, pee * 8)) ||
+        (e = cudaMalloc(&L->d_out, (cp3::kLLMaxParams + 1) * 8)) || (e = cudaMalloc(&L->d_rhoye, (cp3::kMaxRows + 1) * 8)) ||
+        (e = cudaMalloc((void**)&L->d_osc, sizeof(cp3::OscParams))))
+        return lcuda(e, "cudaMalloc(loglik)");
+    // capture
+    cudaStream_t cs;
+    if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking))) return lcuda(e, "cudaStreamCreate");
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    const cp3::LLArgs a = ll_args(L, type);
+    if (!e) e = cudaMemcpyAsync(L->d_osc, L->h_up, sizeof(cp3::OscParams), cudaMemcpyHostToDevice, cs);
+    if (!e)
+        e = cudaMemcpyAsync(L->d_rhoye, L->h_up + sizeof(cp3::OscParams), sizeof(double) * L->nl, cudaMemcpyHostToDevice, cs);
+    if (!e) {
+        const int eb = std::max(1, 256 / L->nl);
+        const int nbE = (L->n_en_pad + eb - 1) / eb;
+        const int nbC = (L->n_cos + L->nl * eb - 1) / (L->nl * eb);
+        cp3::ll_prep_kernel<<<nbE + nbC, dim3(L->nl, eb), (size_t)eb * L->nl * 9 * 8, cs>>>(a);
+        e = cudaGetLastError();
+    }
+    if (!e) {
+        dim3 grid((L->n_en + 3) / 4, L->n_cchunk);
+        if (L->mixed)
+            cp3::ll_pair_kernel<float><<<grid, 128, 0, cs>>>(a);
+        else
+            cp3::ll_pair_kernel<double><<<grid, 128, 0, cs>>>(a);
+        e = cudaGetLastError();
+    }
+    if (!e) {
+        cp3::ll_reduce_kernel<<<1, 256, 0, cs>>>(a);
+        e = cudaGetLastError();
+    }
+    if (!e) e = cudaMemcpyAsync(L->h_out, L->d_out, sizeof(double) * (7 + L->n_rows), cudaMemcpyDeviceToHost, cs);
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+    cudaStreamDestroy(cs);
+    if (e || e2) {
+        if (g) cudaGraphDestroy(g);
+        return lcuda(e ? e : e2, "loglik graph capture");
+    }
+    L->graph = g;
+    if ((e = cudaGraphInstantiate(&L->exec, g, 0))) return lcuda(e, "cudaGraphInstantiate");
+    L->graph_type = type;
+    L->dirty = false;
+    return CP3_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cp3_loglik_create(cp3_loglik** out, int device_id, int precision, int n_cos, int n_en) {
+    if (!out) return lfail(CP3_ERR_ARGUMENT, "cp3_loglik_create: null output pointer");
+    *out = nullptr;
+    if (n_cos <= 0 || n_en <= 0) return lfail(CP3_ERR_ARGUMENT, "cp3_loglik_create: empty binning");
+    if (precision != CP3_PRECISION_FP64 && precision != CP3_PRECISION_MIXED)
+        return lfail(CP3_ERR_ARGUMENT, "cp3_loglik_create: unknown precision");
+    if (device_id < 0 || device_id >= cp3_device_count()) return lfail(CP3_ERR_NO_DEVICE, "No GPU found");
+    LGuard g(device_id);
+    if (g.err) return lcuda(g.err, "cudaSetDevice");
+    cp3_loglik* L = new cp3_loglik();
+    L->device = device_id;
+    L->mixed = precision == CP3_PRECISION_MIXED;
+    L->n_cos = n_cos;
+    L->n_en = n_en;
+    L->maxl.assign(n_cos, 0);
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking)) ||
+        (e = cudaMallocHost((void**)&L->h_up, up_bytes(L))) ||
+        (e = cudaMallocHost((void**)&L->h_out, sizeof(double) * (cp3::kLLMaxParams + 1)))) {
+        int rc = lcuda(e, "loglik create");
+        cp3_loglik_destroy(L);
+        return rc;
+    }
+    *out = L;
+    return CP3_OK;
+}
+
+int cp3_loglik_destroy(cp3_loglik* L) {
+    if (!L) return CP3_OK;
+    LGuard g(L->device);
+    if (L->stream) cudaStreamSynchronize(L->stream);
+    ll_free(L);
+    if (L->h_up) cudaFreeHost(L->h_up);
+    if (L->h_out) cudaFreeHost(L->h_out);
+    if (L->stream) cudaStreamDestroy(L->stream);
+    delete L;
+    return CP3_OK;
+}
+
+int cp3_loglik_set_bins(cp3_loglik* L, const double* cosines, const double* energies) {
+    if (!L || !cosines || !energies) return lfail(CP3_ERR_ARGUMENT, "null argument");
+    for (int i = 0; i < L->n_cos; i++)
+        if (!(cosines[i] >= -1.0 && cosines[i] <= 1.0)) return lfail(CP3_ERR_ARGUMENT, "cosines must lie in [-1, 1]");
+    for (int i = 0; i < L->n_en; i++)
+        if (!(energies[i] > 0.0) || !std::isfinite(energies[i]))
+            return lfail(CP3_ERR_ARGUMENT, "energies must be finite and positive");
+    L->cosines.assign(cosines, cosines + L->n_cos);
+    L->energies.assign(energies, energies + L->n_en);
+    L->has_bins = true;
+    L->dirty = true;
+    return CP3_OK;
+}
+
+int cp3_loglik_set_body(cp3_loglik* L, const double* radii, const double* ye, int n) {
+    if (!L || !radii || n <= 0) return lfail(CP3_ERR_ARGUMENT, "setDensity : vectors must not be empty");
+    if (n > CP3_MAX_ROWS) return lfail(CP3_ERR_LIMIT, "setDensity : more than 64 rows");
+    bool flip = false;
+    if (n >= 2) {
+        const int sign = (radii[1] - radii[0] > 0 ? 1 : -1);
+        for (int i = 1; i < n; i++)
+            if ((radii[i] - radii[i - 1]) * sign < 0) return lfail(CP3_ERR_ARGUMENT, "radii order messed up");
+        flip = sign == 1;
+    }
+    L->radii.resize(n);
+    L->ye.resize(n);
+    L->layer_row.assign(n + 1, -1);
+    for (int i = 0; i < n; i++) {
+        const int s = flip ? n - 1 - i : i;
+        L->radii[i] = radii[s];
+        L->ye[i] = ye ? ye[s] : 0.5;
+        L->layer_row[i + 1] = s;
+    }
+    L->coslimit.resize(n);
+    for (int i = 0; i < n; i++) {
+        double x = -1 * std::sqrt(1 - (L->radii[i] * L->radii[i] / (cp3::kREarth * cp3::kREarth)));
+        if (i == 0) x = 0;
+        L->coslimit[i] = x;
+    }
+    L->n_rows = n;
+    L->has_body = true;
+    L->dirty = true;
+    return CP3_OK;
+}
+
+int cp3_loglik_set_production_height(cp3_loglik* L, double km) {
+    if (!L || !std::isfinite(km)) return lfail(CP3_ERR_ARGUMENT, "setProductionHeight: height must be finite");
+    L->height_cm = km * 100000.0;
+    L->has_height = true;
+    L->dirty = true;
+    return CP3_OK;
+}
+
+int cp3_loglik_set_flux(cp3_loglik* L, const double* flux_e, const double* flux_mu, double norm) {
+    if (!L || !flux_e || !flux_mu || !std::isfinite(norm)) return lfail(CP3_ERR_ARGUMENT, "bad flux");
+    L->flux_e.assign(flux_e, flux_e + L->n_en);
+    L->flux_mu.assign(flux_mu, flux_mu + L->n_en);
+    L->norm = norm;
+    L->has_flux = true;
+    L->dirty = true;
+    return CP3_OK;
+}
+
+int cp3_loglik_set_observed(cp3_loglik* L, const double* counts) {
+    if (!L || !counts) return lfail(CP3_ERR_ARGUMENT, "null counts");
+    L->counts.assign(counts, counts + (size_t)L->n_cos * L->n_en);
+    L->has_counts = true;
+    L->dirty = true;
+    return CP3_OK;
+}
+
+int cp3_loglik_evaluate(cp3_loglik* L, int type, const double* params, const double* rhos, double* loglik,
+                        double* grad) {
+    if (!L || !params || !rhos) return lfail(CP3_ERR_ARGUMENT, "null argument");
+    if (!L->has_bins || !L->has_body || !L->has_flux || !L->has_counts || !L->has_height)
+        return lfail(CP3_ERR_STATE, "loglik: bins, body, flux, observed counts and production height must be set");
+    if (type != CP3_NEUTRINO && type != CP3_ANTINEUTRINO) return lfail(CP3_ERR_ARGUMENT, "unknown neutrino type");
+    for (int k = 0; k < 6; k++)
+        if (!std::isfinite(params[k])) return lfail(CP3_ERR_ARGUMENT, "loglik: parameters must be finite");
+    for (int r = 0; r < L->n_rows; r++)
+        if (!(rhos[r] >= 0.0)) return lfail(CP3_ERR_ARGUMENT, "loglik: densities must be >= 0");
+    LGuard g(L->device);
+    cudaGetLastError();  // a failed earlier call must not be reported below
+    if (L->dirty || type != L->graph_type) {
+        if (int rc = ll_setup(L, type)) return rc;
+    }
+    // parameters into the pinned staging buffer (read by the graph's first copies)
+    cp3::OscParams o{};
+    {
+        double mv[3] = {0.0, params[4], params[4] + params[5]};
+        if (params[4] == 0.0) mv[0] -= 5.0e-9;
+        if (params[5] == 0.0) mv[2] += 5.0e-9;
+        o.dm01 = mv[0] - mv[1];
+        o.dm02 = mv[0] - mv[2];
+        o.d1 = -o.dm01;
+        o.d2 = -o.dm02;
+        const double s12 = std::sin(params[0]), c12 = std::cos(params[0]);
+        const double s13 = std::sin(params[1]), c13 = std::cos(params[1]);
+        o.u00 = (c12 * c13) * (c12 * c13);
+        o.u01 = (s12 * c13) * (s12 * c13);
+        o.u02 = s13 * s13;
+        const double O[9] = {c13 * c12, c13 * s12, s13, -s12, c12, 0.0, -s13 * c12, -s13 * s12, c13};
+        std::memcpy(o.o, O, sizeof O);
+        o.s23 = std::sin(params[2]);
+        o.c23 = std::cos(params[2]);
+        o.sd = std::sin(params[3]);
+        o.cd = std::cos(params[3]);
+        o.anti = type == CP3_ANTINEUTRINO;
+    }
+    std::memcpy(L->h_up, &o, sizeof o);
+    double* rhoye = (double*)(L->h_up + sizeof(cp3::OscParams));
+    rhoye[0] = 0.0;
+    for (int l = 1; l < L->nl; l++) rhoye[l] = rhos[L->layer_row[l]] * L->ye[l - 1];
+    cudaError_t e = cudaGraphLaunch(L->exec, L->stream);
+    if (!e) e = cudaStreamSynchronize(L->stream);
+    if (e) return lcuda(e, "loglik evaluation");
+    if (loglik) *loglik = L->h_out[0];
+    if (grad)
+        for (int q = 0; q < 6 + L->n_rows; q++) grad[q] = L->h_out[1 + q];
+    return CP3_OK;
+}
+
+}  // extern "C"

@@ -197,6 +197,31 @@ int cp3_batch_result_device_ptr(cp3_batch* b, void** dptr);
 int cp3_batch_copy_results_to_host(cp3_batch* b, void* dst, size_t bytes);
 int cp3_batch_get_maxlayers(cp3_batch* b, int* out, long long n);
 
+/* ------------------------------------------------------ log-likelihood
+ * Binned Poisson log-likelihood of the propagated probabilities and its
+ * gradient by a hand-written adjoint.  Bin (c, e) expects
+ *   lambda = norm * (flux_e[e] P(e -> mu) + flux_mu[e] P(mu -> mu))
+ * events and LL = sum n ln(lambda) - lambda.  The gradient is with respect to
+ * theta12, theta13, theta23, dcp, dm12sq, dm23sq and the density of every row
+ * of the body (in the order given to cp3_loglik_set_body).  The per-layer
+ * matrices are recomputed in the backward pass, not stored.  No reference
+ * counterpart (the reference computes probabilities only). */
+typedef struct cp3_loglik cp3_loglik;
+
+int cp3_loglik_create(cp3_loglik** out, int device_id, int precision, int n_cosines, int n_energies);
+int cp3_loglik_destroy(cp3_loglik* L);
+int cp3_loglik_set_bins(cp3_loglik* L, const double* cosines, const double* energies);
+/* radii (any monotone order, as setDensity) and electron fractions (NULL: 0.5) */
+int cp3_loglik_set_body(cp3_loglik* L, const double* radii, const double* ye, int n);
+int cp3_loglik_set_production_height(cp3_loglik* L, double height_km);
+int cp3_loglik_set_flux(cp3_loglik* L, const double* flux_e, const double* flux_mu, double norm);
+/* observed counts, [n_cosines][n_energies] */
+int cp3_loglik_set_observed(cp3_loglik* L, const double* counts);
+/* params: theta12, theta13, theta23, dcp, dm12sq, dm23sq; rhos: one per row.
+ * grad (may be NULL) receives 6 + n_rows values. */
+int cp3_loglik_evaluate(cp3_loglik* L, int type, const double* params, const double* rhos,
+                        double* loglik, double* grad);
+
 #ifdef __cplusplus
 }
 #endif
