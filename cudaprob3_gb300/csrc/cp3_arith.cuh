@@ -89,6 +89,18 @@ struct Q30 {
         i = mad(a2.im, b2.re, i);
         return C{rnd(r), rnd(i)};
     }
+    // conj(a0 b1 - a1 b0): one component of conj(u x v)
+    __device__ __forceinline__ C crossConj(C a0, C a1, C b0, C b1) const {
+        long long r = mul(a0.re, b1.re);
+        r = mad(-a0.im, b1.im, r);
+        r = mad(-a1.re, b0.re, r);
+        r = mad(a1.im, b0.im, r);
+        long long i = mul(-a0.re, b1.im);
+        i = mad(-a0.im, b1.re, i);
+        i = mad(a1.re, b0.im, i);
+        i = mad(a1.im, b0.re, i);
+        return C{rnd(r), rnd(i)};
+    }
     // c*x + s*y  and  -s*x + c*y  for a real rotation of two complex numbers
     __device__ __forceinline__ void rot(R c, R s, C& x, C& y) const {
         const int ns = -s;
@@ -133,12 +145,9 @@ struct Q30 {
 //      they are added to the exact Q1.30 table entry.
 // `tab` holds 257 entries (Q1.30 cos, Q1.30 sin, float cos, float sin) for
 // j = -128..128 at index j + 128.
-__device__ __forceinline__ void phase_q30(float kh, float kl, float Lh, float Ll,
-                                          const int4* __restrict__ tab, int& cq, int& sq) {
-    const float p = kh * Lh;
-    float e = fmaf(kh, Lh, -p);
-    e = fmaf(kh, Ll, e);
-    e = fmaf(kl, Lh, e);
+// Q1.30 cos/sin of 2 pi (p + e) for a phase given in turns as a double-float
+// pair (|e| small against 1): steps 2-4 above.
+__device__ __forceinline__ void turns_q30(float p, float e, const int4* __restrict__ tab, int& cq, int& sq) {
     const float u = p - rintf(p);
     float j = rintf(u * 256.0f);
     j = fminf(fmaxf(j, -128.0f), 128.0f);
@@ -155,6 +164,36 @@ __device__ __forceinline__ void phase_q30(float kh, float kl, float Lh, float Ll
     cq = t.x + __float2int_rn(dc * 1073741824.0f);
     sq = t.y + __float2int_rn(ds * 1073741824.0f);
 }
+
+// t = (kh + kl) (Lh + Ll) turns as p + e: p = kh*Lh rounded, e its exact
+// rounding error plus the cross terms (step 1 above).
+__device__ __forceinline__ void turns_product(float kh, float kl, float Lh, float Ll, float& p, float& e) {
+    p = kh * Lh;
+    e = fmaf(kh, Lh, -p);
+    e = fmaf(kh, Ll, e);
+    e = fmaf(kl, Lh, e);
+}
+
+__device__ __forceinline__ void phase_q30(float kh, float kl, float Lh, float Ll, const int4* __restrict__ tab,
+                                          int& cq, int& sq) {
+    float p, e;
+    turns_product(kh, kl, Lh, Ll, p, e);
+    turns_q30(p, e, tab, cq, sq);
+}
+
+// Double-float running sum of phases in turns, kept reduced to [-1/2, 1/2]:
+// only e^{2 pi i sum} is needed, and the reduction keeps the pair exact.
+struct TurnSum {
+    float h = 0.0f, l = 0.0f;
+    __device__ __forceinline__ void add(float p, float e) {
+        p -= rintf(p);  // exact
+        const float s = h + p;
+        const float bp = s - h;
+        const float err = (h - (s - bp)) + (p - bp);  // two-sum
+        h = s - rintf(s);
+        l += err + e;
+    }
+};
 
 // ------------------------------------------------------------------ FP64 ----
 struct F64 {
@@ -190,6 +229,12 @@ struct F64 {
         i = fma(a2.re, b2.im, i);
         i = fma(a2.im, b2.re, i);
         return C{r, i};
+    }
+    // conj(a0 b1 - a1 b0)
+    static __device__ __forceinline__ C crossConj(C a0, C a1, C b0, C b1) {
+        const double re = fma(a0.re, b1.re, -a0.im * b1.im) - fma(a1.re, b0.re, -a1.im * b0.im);
+        const double im = fma(a0.re, b1.im, a0.im * b1.re) - fma(a1.re, b0.im, a1.im * b0.re);
+        return C{re, -im};
     }
     static __device__ __forceinline__ void rot(R c, R s, C& x, C& y) {
         const C nx{fma(c, x.re, s * y.re), fma(c, x.im, s * y.im)};

@@ -22,6 +22,8 @@ namespace cp3 {
 
 // Src provides, for the current pair:
 //   void phase(int l, R& c1, R& s1, R& n1, R& c2, R& s2, R& n2)  e^{i psi_k}, n = -s
+//   void phase_acc(..., Turns& acc)   the same, adding psi_1 + psi_2 (turns) to acc
+//   void turns_phase(const Turns& acc, R& c, R& s)               e^{2 pi i acc}
 //   R T(int l, int i, int j)     overlap V_{l+1}^T V_l
 //   R La(int j)                  row 0 of W V_1 (real)
 //   C Lb(int j)                  row 1 of W V_1
@@ -63,20 +65,24 @@ __device__ __forceinline__ void flavour_block(const P& ar, const Src& src, int M
     }
     C Y[9];
     if (M >= 2) {
-        src.phase(1, c1, s1, n1, c2, s2, n2);
+        // Only columns 0 and 1 of Y are propagated; Y is unitary with
+        // det Y = prod_l det(T_l) det(D_l) = e^{2 pi i sum_l (t1 + t2)_l}
+        // (right-handed eigen-bases make det T_l = 1), so column 2 is
+        // det(Y) conj(col0 x col1).
+        typename Src::Turns phi;
+        src.phase_acc(1, c1, s1, n1, c2, s2, n2, phi);
 #pragma unroll
         for (int i = 0; i < 3; i++) {
             Y[3 * i] = P::creal(src.T(1, i, 0));
             Y[3 * i + 1] = ar.mulRC(src.T(1, i, 1), C{c1, s1});
-            Y[3 * i + 2] = ar.mulRC(src.T(1, i, 2), C{c2, s2});
         }
         for (int l = 2; l < M; l++) {
-            src.phase(l, c1, s1, n1, c2, s2, n2);
+            src.phase_acc(l, c1, s1, n1, c2, s2, n2, phi);
             const R t00 = src.T(l, 0, 0), t01 = src.T(l, 0, 1), t02 = src.T(l, 0, 2);
             const R t10 = src.T(l, 1, 0), t11 = src.T(l, 1, 1), t12 = src.T(l, 1, 2);
             const R t20 = src.T(l, 2, 0), t21 = src.T(l, 2, 1), t22 = src.T(l, 2, 2);
 #pragma unroll
-            for (int j = 0; j < 3; j++) {
+            for (int j = 0; j < 2; j++) {
                 const C z0 = Y[j];
                 const C z1 = ar.mulPhase(Y[3 + j], c1, s1, n1);
                 const C z2 = ar.mulPhase(Y[6 + j], c2, s2, n2);
@@ -85,6 +91,11 @@ __device__ __forceinline__ void flavour_block(const P& ar, const Src& src, int M
                 Y[6 + j] = ar.dotRC(t20, t21, t22, z0, z1, z2);
             }
         }
+        R dc, ds;
+        src.turns_phase(phi, dc, ds);
+        Y[2] = ar.mulPhase(ar.crossConj(Y[3], Y[6], Y[4], Y[7]), dc, ds, -ds);
+        Y[5] = ar.mulPhase(ar.crossConj(Y[6], Y[0], Y[7], Y[1]), dc, ds, -ds);
+        Y[8] = ar.mulPhase(ar.crossConj(Y[0], Y[3], Y[1], Y[4]), dc, ds, -ds);
     } else {
 #pragma unroll
         for (int i = 0; i < 9; i++) Y[i] = P::cz();

@@ -86,6 +86,15 @@ CP3_HD void layer_eigen(const OscParams& p, double E, double rhoye, double m[3],
         V[3 + k] = v1 * inv;
         V[6 + k] = v2 * inv;
     }
+    // right-handed basis (det V = +1): every overlap T_l = V_{l+1}^T V_l is then a
+    // rotation, which the propagation kernels rely on to rebuild a column
+    const double det = V[0] * (V[4] * V[8] - V[5] * V[7]) - V[1] * (V[3] * V[8] - V[5] * V[6]) +
+                       V[2] * (V[3] * V[7] - V[4] * V[6]);
+    if (det < 0.0) {
+        V[2] = -V[2];
+        V[5] = -V[5];
+        V[8] = -V[8];
+    }
 }
 
 // Phase rate of eigenvalue k relative to eigenvalue 0, in turns per km:

@@ -130,6 +130,24 @@ struct MixedSrc {
         n1 = -s1;
         n2 = -s2;
     }
+    using Turns = TurnSum;
+    __device__ __forceinline__ void phase_acc(int l, int& c1, int& s1, int& n1, int& c2, int& s2, int& n2,
+                                              Turns& acc) const {
+        const float2 L = len[l];
+        const int* k = tab + (l * kMixedWords + 9) * TE;
+        float p1, e1, p2, e2;
+        turns_product(__int_as_float(k[0]), __int_as_float(k[TE]), L.x, L.y, p1, e1);
+        turns_product(__int_as_float(k[2 * TE]), __int_as_float(k[3 * TE]), L.x, L.y, p2, e2);
+        turns_q30(p1, e1, ptab, c1, s1);
+        turns_q30(p2, e2, ptab, c2, s2);
+        acc.add(p1, e1);
+        acc.add(p2, e2);
+        n1 = -s1;
+        n2 = -s2;
+    }
+    __device__ __forceinline__ void turns_phase(const Turns& acc, int& c, int& s) const {
+        turns_q30(acc.h, acc.l, ptab, c, s);
+    }
 };
 
 template <int TE>
@@ -150,6 +168,21 @@ struct F64Src {
         phase_f64(k[TE], L, c2, s2);
         n1 = -s1;
         n2 = -s2;
+    }
+    struct Turns {
+        double t = 0.0;  // reduced to [-1/2, 1/2]
+    };
+    __device__ __forceinline__ void phase_acc(int l, double& c1, double& s1, double& n1, double& c2, double& s2,
+                                              double& n2, Turns& acc) const {
+        phase(l, c1, s1, n1, c2, s2, n2);
+        const double L = len[l];
+        const double* k = tab + (l * kFp64Words + 9) * TE;
+        const double t1 = k[0] * L, t2 = k[TE] * L;
+        acc.t += (t1 - rint(t1)) + (t2 - rint(t2));
+        acc.t -= rint(acc.t);
+    }
+    __device__ __forceinline__ void turns_phase(const Turns& acc, double& c, double& s) const {
+        sincospi(2.0 * acc.t, &s, &c);
     }
 };
 
