@@ -95,11 +95,12 @@ def grid():
 # ------------------------------------------------------------- work units --
 def madw_per_pair(M):
     """mad.wide.s32 operations one pair executes in the mixed kernel
-    (flavour_block in cp3_chain.cuh): 78 per inner chain step T_l D_l, and the
-    fixed cost of D_0 Gamma', T_0 (.), G = Y^T D_M Y, G X', Lambda' X and the
-    four exact |S|^2 of the 2x2 flavour block."""
+    (flavour_block in cp3_chain.cuh): 52 per inner chain step T_l D_l on two
+    columns, 36 to rebuild the third column, and the fixed cost of D_0 Gamma',
+    T_0 (.), G = Y^T D_M Y, G X', Lambda' X and the four exact |S|^2 of the
+    2x2 flavour block."""
     M = np.asarray(M, dtype=np.int64)
-    return np.where(M >= 2, 78 * M + 116, np.where(M == 1, 260, 68))
+    return np.where(M >= 2, 52 * M + 198, np.where(M == 1, 260, 68))
 
 
 def survey_flops_per_pair(M):
