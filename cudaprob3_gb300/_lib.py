@@ -82,6 +82,8 @@ SIGNATURES = [
     ("cp3_loglik_set_flux", _I, [_P, _DP, _DP, _D]),
     ("cp3_loglik_set_observed", _I, [_P, _DP]),
     ("cp3_loglik_evaluate", _I, [_P, _I, _DP, _DP, _DP, _DP]),
+    ("cp3_propagate_noalloc", _I, [_I, _I, _P, _I, _P, _I, _DP, _DP, _DP, _I, _D, _D, _D, _D, _D, _D, _D, _P,
+                                   _P]),
 ]
 
 PIPE_IMAD_WIDE = 0

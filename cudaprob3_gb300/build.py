@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcudaprob3_gb300.so")
-SOURCES = ["cp3_abi.cu", "cp3_kernels.cu", "cp3_pipes.cu", "cp3_batch.cu", "cp3_loglik.cu"]
+SOURCES = ["cp3_abi.cu", "cp3_kernels.cu", "cp3_pipes.cu", "cp3_batch.cu", "cp3_loglik.cu", "cp3_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr",
               "-I" + os.path.join(ROOT, "include")]

@@ -1,0 +1,235 @@
+// One calculation that allocates nothing: cp3_propagate_noalloc.
+//
+// Some callers cannot call cudaMalloc: code that runs while a stream is being
+// captured into a CUDA graph (allocation is not a capturable operation),
+// callers inside a framework whose caching allocator must own every device
+// byte, and latency-bound or real-time loops that may not take the implicit
+// device synchronisation of cudaMalloc/cudaFree.  For them this entry point
+// runs the single-grid calculation (precompute, then propagation) on the
+// caller's device pointers and stream, with its scratch tables in a
+// file-scope __device__ array instead of per-handle allocations.
+//
+// The array is sized for grids up to kNoAllocMaxCosines x kNoAllocMaxEnergies
+// and kNoAllocMaxRows density rows, in either precision (about 14 MB); every
+// GPU that loads the library holds it until the process exits.  All calls on
+// one device share it: every region is rewritten before it is read, so no call
+// depends on a previous one, but calls whose work overlaps on the GPU (other
+// streams, other host threads) race on it and must be serialised by the caller.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <mutex>
+#include <string>
+
+#include "../../include/cudaprob3_gb300.h"
+#include "cp3_launch.h"
+#include "cp3_tile.cuh"
+
+namespace cp3 {
+
+constexpr int kNoAllocMaxCosines = CP3_NOALLOC_MAX_COSINES;
+constexpr int kNoAllocMaxEnergies = CP3_NOALLOC_MAX_ENERGIES;
+constexpr int kNoAllocMaxRows = CP3_NOALLOC_MAX_ROWS;
+constexpr int kNoAllocMaxLayers = kNoAllocMaxRows + 1;  // vacuum + rows
+constexpr int kNoAllocLayersPad = (kNoAllocMaxLayers + 1) / 2 * 2;
+
+constexpr size_t align256(size_t b) { return (b + 255) / 256 * 256; }
+// regions (bytes) for the largest problem; FP64 words are the larger ones
+constexpr size_t kNaTab = align256((size_t)kNoAllocMaxEnergies * kNoAllocMaxLayers * kFp64Words * 8);
+constexpr size_t kNaPe = align256((size_t)kPerEWords * kNoAllocMaxEnergies * 8);
+constexpr size_t kNaLen = align256((size_t)kNoAllocMaxCosines * kNoAllocLayersPad * 8);
+constexpr size_t kNaMaxl = align256((size_t)kNoAllocMaxCosines * 4);
+constexpr size_t kNaPhase = align256((size_t)kPhaseTabBytes);
+constexpr size_t kNaBody = align256((size_t)2 * kNoAllocMaxLayers * 8);  // radii, rho*Ye
+constexpr size_t kNaBytes = kNaTab + kNaPe + kNaLen + kNaMaxl + kNaPhase + kNaBody;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+struct NoAllocBody {
+    int n;                              // rows
+    double radii[kNoAllocMaxRows];      // outside-in
+    double rhoye[kNoAllocMaxLayers];    // layer 0 = vacuum
+    double coslimit[kNoAllocMaxRows];   // propagator.hpp:149-158
+};
+
+// Writes the layer radii and densities, the Q1.30/float cos-sin table and the
+// layer count of every cosine (propagator.hpp:301-307) into the scratch.
+__global__ void noalloc_setup_kernel(NoAllocBody body, const double* cosines, int n_cos, double* radii,
+                                     double* rhoye, int4* ptab, int* maxl) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < body.n) radii[t] = body.radii[t];
+    if (t <= body.n) rhoye[t] = body.rhoye[t];
+    if (t <= kPhaseTabN) {
+        double s, c;
+        sincospi((double)(t - kPhaseTabN / 2) / (kPhaseTabN / 2), &s, &c);
+        ptab[t] = make_int4((int)__double2ll_rn(c * 1073741824.0), (int)__double2ll_rn(s * 1073741824.0),
+                            __float_as_int(__double2float_rn(c)), __float_as_int(__double2float_rn(s)));
+    }
+    if (t < n_cos) {
+        const double cz = cosines[t];
+        int cnt = 0;
+        for (int i = 0; i < body.n; i++) cnt += (cz < body.coslimit[i]);
+        maxl[t] = cnt;
+    }
+}
+
+}  // namespace cp3
+
+namespace {
+
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[256] = {};
+
+int nfail(int code, const std::string& m) {
+    cp3::set_last_error(m);
+    return code;
+}
+
+}  // namespace
+
+extern "C" int cp3_propagate_noalloc(int precision, int type, const double* d_cosines, int n_cosines,
+                                     const double* d_energies, int n_energies, const double* radii,
+                                     const double* rhos, const double* ye, int n_rows, double theta12,
+                                     double theta13, double theta23, double dcp, double dm12sq, double dm23sq,
+                                     double height_km, void* d_out, void* stream) {
+    using namespace cp3;
+    if (precision != CP3_PRECISION_FP64 && precision != CP3_PRECISION_MIXED)
+        return nfail(CP3_ERR_ARGUMENT, "propagate_noalloc: unknown precision");
+    if (type != CP3_NEUTRINO && type != CP3_ANTINEUTRINO)
+        return nfail(CP3_ERR_ARGUMENT, "propagate_noalloc: unknown neutrino type");
+    if (n_cosines < 0 || n_energies < 0 || n_cosines > kNoAllocMaxCosines || n_energies > kNoAllocMaxEnergies)
+        return nfail(CP3_ERR_LIMIT, "propagate_noalloc: grid larger than " + std::to_string(kNoAllocMaxCosines) +
+                                        " cosines x " + std::to_string(kNoAllocMaxEnergies) + " energies");
+    if (n_rows <= 0) return nfail(CP3_ERR_ARGUMENT, "setDensity : vectors must not be empty");
+    if (n_rows > kNoAllocMaxRows)
+        return nfail(CP3_ERR_LIMIT, "propagate_noalloc: more than " + std::to_string(kNoAllocMaxRows) + " density rows");
+    if (!radii || !rhos || (n_cosines && !d_cosines) || (n_energies && !d_energies) ||
+        (n_cosines && n_energies && !d_out))
+        return nfail(CP3_ERR_ARGUMENT, "propagate_noalloc: null pointer");
+    const double par[7] = {theta12, theta13, theta23, dcp, dm12sq, dm23sq, height_km};
+    for (double v : par)
+        if (!std::isfinite(v)) return nfail(CP3_ERR_ARGUMENT, "propagate_noalloc: parameters must be finite");
+    // setDensity (propagator.hpp:117-161): one monotone order, outside-in
+    NoAllocBody body{};
+    body.n = n_rows;
+    bool flip = false;
+    if (n_rows >= 2) {
+        const int sign = (radii[1] - radii[0] > 0 ? 1 : -1);
+        for (int i = 1; i < n_rows; i++)
+            if ((radii[i] - radii[i - 1]) * sign < 0) return nfail(CP3_ERR_ARGUMENT, "radii order messed up");
+        flip = sign == 1;
+    }
+    body.rhoye[0] = 0.0;
+    for (int i = 0; i < n_rows; i++) {
+        const int s = flip ? n_rows - 1 - i : i;
+        const double y = ye ? ye[s] : 0.5;
+        if (!(radii[s] >= 0.0) || !(rhos[s] >= 0.0) || !(y >= 0.0 && y <= 1.0))
+            return nfail(CP3_ERR_ARGUMENT, "setDensity : bad radius, density or electron fraction");
+        body.radii[i] = radii[s];
+        body.rhoye[i + 1] = rhos[s] * y;
+        double x = -1 * std::sqrt(1 - (body.radii[i] * body.radii[i] / (kREarth * kREarth)));
+        if (i == 0) x = 0;
+        body.coslimit[i] = x;
+    }
+    if (n_cosines == 0 || n_energies == 0) return CP3_OK;
+
+    // set-up once per device, with that device current: the device address of
+    // the scratch array (its host-side name is not a device address)
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return nfail(CP3_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    if (dev < 0 || dev >= 256) return nfail(CP3_ERR_NO_DEVICE, "propagate_noalloc: device id out of range");
+    void* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!g_noalloc_ptr[dev]) {
+            e = cudaGetSymbolAddress(&g_noalloc_ptr[dev], g_noalloc_scratch);
+            if (e != cudaSuccess) {
+                g_noalloc_ptr[dev] = nullptr;
+                return nfail(CP3_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+            }
+        }
+        base = g_noalloc_ptr[dev];
+    }
+    unsigned char* sc = (unsigned char*)base;
+    void* tab = sc;
+    void* pe = sc + kNaTab;
+    void* len = sc + kNaTab + kNaPe;
+    int* maxl = (int*)(sc + kNaTab + kNaPe + kNaLen);
+    int4* ptab = (int4*)(sc + kNaTab + kNaPe + kNaLen + kNaMaxl);
+    double* d_radii = (double*)(sc + kNaTab + kNaPe + kNaLen + kNaMaxl + kNaPhase);
+    double* d_rhoye = d_radii + kNoAllocMaxLayers;
+
+    const bool mixed = precision == CP3_PRECISION_MIXED;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaGetLastError();  // an earlier failed call must not be reported by the checks below
+    const int nl = n_rows + 1;
+    const int nl_pad = (nl + 1) / 2 * 2;
+    const int te = 64, groups = mixed ? 4 : 2, cchunk = 32;
+    const int n_en_pad = (n_energies + te - 1) / te * te;
+    {
+        const int n = std::max(n_cosines, kPhaseTabN + 1);
+        noalloc_setup_kernel<<<(n + 255) / 256, 256, 0, s>>>(body, d_cosines, n_cosines, d_radii, d_rhoye, ptab,
+                                                             maxl);
+        if ((e = cudaGetLastError()) != cudaSuccess)
+            return nfail(CP3_ERR_CUDA, std::string("setup kernel: ") + cudaGetErrorString(e));
+    }
+    PrepArgs pa{};
+    pa.pb.n_cos = n_cosines;
+    pa.pb.n_en = n_energies;
+    pa.pb.n_en_pad = n_en_pad;
+    pa.pb.te = te;
+    pa.pb.nl = nl;
+    pa.pb.nl_pad = nl_pad;
+    pa.pb.energies = d_energies;
+    pa.pb.cosines = d_cosines;
+    pa.pb.maxlayers = maxl;
+    pa.pb.radii = d_radii;
+    pa.pb.rhoye = d_rhoye;
+    pa.pb.height_cm = height_km * 100000.0;
+    {
+        // propagator.hpp:191-248
+        double mv[3] = {0.0, dm12sq, dm12sq + dm23sq};
+        if (dm12sq == 0.0) mv[0] -= 5.0e-9;
+        if (dm23sq == 0.0) mv[2] += 5.0e-9;
+        OscParams& o = pa.osc;
+        o.dm01 = mv[0] - mv[1];
+        o.dm02 = mv[0] - mv[2];
+        o.d1 = -o.dm01;
+        o.d2 = -o.dm02;
+        const double s12 = std::sin(theta12), c12 = std::cos(theta12);
+        const double s13 = std::sin(theta13), c13 = std::cos(theta13);
+        o.u00 = (c12 * c13) * (c12 * c13);
+        o.u01 = (s12 * c13) * (s12 * c13);
+        o.u02 = s13 * s13;
+        const double O[9] = {c13 * c12, c13 * s12, s13, -s12, c12, 0.0, -s13 * c12, -s13 * s12, c13};
+        for (int i = 0; i < 9; i++) o.o[i] = O[i];
+        o.s23 = std::sin(theta23);
+        o.c23 = std::cos(theta23);
+        o.sd = std::sin(dcp);
+        o.cd = std::cos(dcp);
+        o.anti = type == CP3_ANTINEUTRINO ? 1 : 0;
+    }
+    pa.tab = tab;
+    pa.pe = pe;
+    pa.len = len;
+    if ((e = launch_prep(mixed, pa, s)) != cudaSuccess)
+        return nfail(CP3_ERR_CUDA, std::string("prep kernel: ") + cudaGetErrorString(e));
+    PropArgs ka{};
+    ka.tab = tab;
+    ka.pe = pe;
+    ka.len = len;
+    ka.maxl = maxl;
+    ka.ptab = ptab;
+    ka.out = d_out;
+    ka.n_cos = n_cosines;
+    ka.n_en = n_energies;
+    ka.n_en_pad = n_en_pad;
+    ka.nl = nl;
+    ka.nl_pad = nl_pad;
+    ka.cchunk = cchunk;
+    const size_t smem = propagate_smem_bytes(mixed, te, nl, nl_pad, cchunk);
+    if ((e = launch_propagate(mixed, ka, te, groups, smem, s)) != cudaSuccess)
+        return nfail(CP3_ERR_CUDA, std::string("propagate kernel: ") + cudaGetErrorString(e));
+    return CP3_OK;
+}

@@ -222,6 +222,37 @@ int cp3_loglik_set_observed(cp3_loglik* L, const double* counts);
 int cp3_loglik_evaluate(cp3_loglik* L, int type, const double* params, const double* rhos,
                         double* loglik, double* grad);
 
+/* ------------------------------------------------------------- no allocation
+ * One calculation that allocates nothing, for callers that cannot call
+ * cudaMalloc: code running while a stream is captured into a CUDA graph,
+ * callers whose framework allocator must own all device memory, and
+ * latency-bound loops that cannot take the device synchronisation of
+ * cudaMalloc/cudaFree.  No counterpart in the reference (its
+ * CudaPropagatorSingle allocates in its constructor, cudapropagator.cuh:73-79).
+ *
+ * Runs on the current device and `stream` (NULL: the default stream).  Inputs
+ * d_cosines[n_cosines] and d_energies[n_energies] and the output
+ * d_out[9][n_cosines][n_energies] (float for CP3_PRECISION_MIXED, double for
+ * CP3_PRECISION_FP64, plane in*3+out as cp3_result_device_ptr) are device
+ * memory owned by the caller; radii/rhos/ye (ye may be NULL: 0.5) are host
+ * arrays read during the call, with the semantics of cp3_set_density.  Results
+ * equal those of cp3_create ... cp3_calculate_probabilities on the same inputs.
+ * Scratch lives in one static device array sized for the limits below (about
+ * 14 MB, held by every GPU that loads the library until exit); larger problems
+ * are rejected with CP3_ERR_LIMIT.  The first call on a device looks up that
+ * array's device address (cudaGetSymbolAddress), so make it before any stream
+ * capture.  Calls share the array: calls whose work overlaps on the GPU race
+ * and must be serialised by the caller.  The call is asynchronous with respect
+ * to the host. */
+#define CP3_NOALLOC_MAX_COSINES 8192
+#define CP3_NOALLOC_MAX_ENERGIES 8192
+#define CP3_NOALLOC_MAX_ROWS 15
+int cp3_propagate_noalloc(int precision, int type, const double* d_cosines, int n_cosines,
+                          const double* d_energies, int n_energies, const double* radii,
+                          const double* rhos, const double* ye, int n_rows, double theta12,
+                          double theta13, double theta23, double dcp, double dm12sq,
+                          double dm23sq, double height_km, void* d_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
