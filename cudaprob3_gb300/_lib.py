@@ -52,6 +52,9 @@ SIGNATURES = [
     ("cp3_set_stream", _I, [_P, _P]),
     ("cp3_last_launch_count", _I, [_P, _IP]),
     ("cp3_get_maxlayers", _I, [_P, _IP, _I]),
+    ("cp3_set_launch_shape", _I, [_P, _I, _I, _I]),
+    ("cp3_get_launch_shape", _I, [_P, _IP, _IP, _IP]),
+    ("cp3_autotune", _I, [_P, _I, _I, _IP, _IP, _IP, ctypes.POINTER(ctypes.c_float)]),
     ("cp3_set_kernel_timing", _I, [_P, _I]),
     ("cp3_last_kernel_ms", _I, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     ("cp3_pipe_peak", _I, [_I, _I, _DP]),

@@ -11,7 +11,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/cudaprob3_gb300.h"
+#include "cudaprob3_gb300.h"
 #include "cp3_launch.h"
 
 namespace {
@@ -585,6 +585,79 @@ int cp3_last_launch_count(cp3_propagator* p, int* launches) {
     if (int rc = check(p)) return rc;
     if (!launches) return fail(CP3_ERR_ARGUMENT, "null output pointer");
     *launches = p->last_launches;
+    return CP3_OK;
+}
+
+int cp3_set_launch_shape(cp3_propagator* p, int te, int groups, int cchunk) {
+    if (int rc = check(p)) return rc;
+    if ((te != 32 && te != 64 && te != 128) || groups < 1 || te * groups > cp3::propagate_max_threads(p->mixed) ||
+        cchunk < 1 || cchunk > 1024)
+        return fail(CP3_ERR_ARGUMENT, "set_launch_shape: unsupported launch shape");
+    p->te = te;
+    p->groups = groups;
+    p->cchunk = cchunk;
+    return CP3_OK;
+}
+
+int cp3_get_launch_shape(cp3_propagator* p, int* te, int* groups, int* cchunk) {
+    if (int rc = check(p)) return rc;
+    if (te) *te = p->te;
+    if (groups) *groups = p->groups;
+    if (cchunk) *cchunk = p->cchunk;
+    return CP3_OK;
+}
+
+// Every supported (te, groups, cchunk) timed on `reps` calculations of this
+// handle's grid (kernel events); the fastest shape is kept.
+int cp3_autotune(cp3_propagator* p, int type, int reps, int* te_out, int* groups_out, int* cchunk_out,
+                 float* best_ms) {
+    if (int rc = check(p)) return rc;
+    if (reps < 1) reps = 1;
+    const bool was_timing = p->timing;
+    if (int rc = cp3_set_kernel_timing(p, 1)) return rc;
+    const int tes[3] = {32, 64, 128};
+    const int chunks[4] = {8, 16, 32, 64};
+    float best = 1e30f;
+    int bt = p->te, bg = p->groups, bc = p->cchunk;
+    int rc = CP3_OK;
+    for (int te : tes)
+        for (int groups = 1; rc == CP3_OK && te * groups <= cp3::propagate_max_threads(p->mixed); groups *= 2) {
+            if (te * groups < 64) continue;
+            for (int cc : chunks) {
+                if (cc < groups) continue;
+                p->te = te;
+                p->groups = groups;
+                p->cchunk = cc;
+                if ((rc = cp3_calculate_probabilities(p, type)) == CP3_ERR_LIMIT) {
+                    rc = CP3_OK;
+                    continue;
+                }
+                if (rc) break;
+                float tot = 0;
+                for (int r = 0; r < reps && rc == CP3_OK; r++) {
+                    float a = 0, b = 0;
+                    if ((rc = cp3_calculate_probabilities(p, type)) == CP3_OK &&
+                        (rc = cp3_last_kernel_ms(p, &a, &b)) == CP3_OK)
+                        tot += a + b;
+                }
+                if (rc) break;
+                if (tot / reps < best) {
+                    best = tot / reps;
+                    bt = te;
+                    bg = groups;
+                    bc = cc;
+                }
+            }
+        }
+    p->te = bt;
+    p->groups = bg;
+    p->cchunk = bc;
+    cp3_set_kernel_timing(p, was_timing ? 1 : 0);
+    if (rc) return rc;
+    if (te_out) *te_out = bt;
+    if (groups_out) *groups_out = bg;
+    if (cchunk_out) *cchunk_out = bc;
+    if (best_ms) *best_ms = best;
     return CP3_OK;
 }
 

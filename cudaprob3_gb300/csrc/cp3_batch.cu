@@ -23,7 +23,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/cudaprob3_gb300.h"
+#include "cudaprob3_gb300.h"
 #include "cp3_launch.h"
 #include "cp3_tile.cuh"
 

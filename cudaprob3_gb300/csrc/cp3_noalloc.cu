@@ -21,7 +21,7 @@
 #include <mutex>
 #include <string>
 
-#include "../../include/cudaprob3_gb300.h"
+#include "cudaprob3_gb300.h"
 #include "cp3_launch.h"
 #include "cp3_tile.cuh"
 

@@ -188,6 +188,22 @@ class CudaPropagatorSingle:
         check(self._lib.cp3_last_kernel_ms(self._h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
+    def set_launch_shape(self, te, groups, cchunk):
+        check(self._lib.cp3_set_launch_shape(self._h, int(te), int(groups), int(cchunk)))
+
+    def launch_shape(self):
+        v = [ctypes.c_int() for _ in range(3)]
+        check(self._lib.cp3_get_launch_shape(self._h, *[ctypes.byref(x) for x in v]))
+        return tuple(x.value for x in v)
+
+    def autotune(self, ntype=0, reps=2):
+        """Time every supported launch shape on this grid; keep the fastest."""
+        te, g, cc = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        ms = ctypes.c_float()
+        check(self._lib.cp3_autotune(self._h, int(ntype), int(reps), ctypes.byref(te), ctypes.byref(g),
+                                     ctypes.byref(cc), ctypes.byref(ms)))
+        return (te.value, g.value, cc.value), ms.value
+
     def last_launch_count(self):
         n = ctypes.c_int()
         check(self._lib.cp3_last_launch_count(self._h, ctypes.byref(n)))

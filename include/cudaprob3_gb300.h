@@ -136,6 +136,16 @@ int cp3_set_stream(cp3_propagator* p, void* cuda_stream);
 /* Kernel launches issued by the last calculation (all are this library's). */
 int cp3_last_launch_count(cp3_propagator* p, int* launches);
 
+/* Launch shape of the propagate kernel: energies per tile te (32, 64, 128),
+ * cosine groups per block, cosines per block (no reference counterpart: the
+ * reference launches 64-thread blocks, cudapropagator.cuh:204-209). */
+int cp3_set_launch_shape(cp3_propagator* p, int te, int groups, int cchunk);
+int cp3_get_launch_shape(cp3_propagator* p, int* te, int* groups, int* cchunk);
+/* Times every supported launch shape on `reps` calculations of this handle's
+ * grid and keeps the fastest (the results of the calculations are valid). */
+int cp3_autotune(cp3_propagator* p, int type, int reps, int* te, int* groups, int* cchunk,
+                 float* best_ms);
+
 /* Layers crossed per cosine (Propagator::maxlayers, propagator.hpp:301-307). */
 int cp3_get_maxlayers(cp3_propagator* p, int* out, int n);
 
