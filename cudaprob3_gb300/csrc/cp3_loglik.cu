@@ -18,10 +18,10 @@
 //                     matrix from the tables (no per-layer storage: the chain is
 //                     un-multiplied with T^T and conj(D)); per-(energy, layer)
 //                     adjoints are summed over the warp's cosines with shuffles
-//   ll_reduce_kernel  one thread per energy: sums the warps' partials,
-//                     re-solves every layer's eigen-problem in FP64 and
-//                     back-propagates through it to the parameters; one block
-//                     sums over energies (fixed order: deterministic)
+//   ll_layer_kernel   one block per energy, one thread per layer: sums the
+//                     warps' partials, re-solves the layer's eigen-problem in
+//                     FP64 and back-propagates through it to the parameters
+//   ll_sum_kernel     sums the per-energy rows (fixed order: deterministic)
 // Precision: FP64 does every step in double; MIXED runs ll_pair_kernel in
 // FP32 (phases in double-float) with the FP64 tables and FP64 reduction.
 #include <cuda_runtime.h>
@@ -114,6 +114,7 @@ struct LLArgs {
     // partials and results
     double* part_l;  // [n_cchunk][n_en][nl][11]
     double* part_e;  // [n_cchunk][n_en][19]
+    double* part_g;  // [n_en][7 + n_rows]: per-energy LL and gradient
     double* out;     // [1 + 6 + nrows]: LL, gradient
     const int* layer_row;  // [nl]: caller's row of layer l (l >= 1), -1 for layer 0
     int n_rows;
@@ -487,157 +488,203 @@ __global__ void __launch_bounds__(128) ll_pair_kernel(LLArgs a) {
 }
 
 // ---------------------------------------------------------- reduction ----
-// Thread e: sum of the partials of energy e, FP64 eigen back-propagation to
-// the parameters; then a fixed-order block sum over energies.
-__global__ void __launch_bounds__(256) ll_reduce_kernel(LLArgs a) {
-    __shared__ double s_acc[256];
-    const int np = 6 + a.n_rows;
-    double grad[kLLMaxParams + 1];  // [0] LL, then the gradient
-    for (int q = 0; q <= np; q++) grad[q] = 0.0;
-    const OscParams o = *a.osc;
-    for (int e = threadIdx.x; e < a.n_en; e += blockDim.x) {
-        const double E = a.energies[e];
-        double gT[kMaxRows + 1][9], gK[kMaxRows + 1][2];
-        double gL[18];
-        for (int l = 0; l < a.nl; l++) {
-            for (int q = 0; q < 9; q++) gT[l][q] = 0.0;
-            gK[l][0] = gK[l][1] = 0.0;
-        }
-        for (int q = 0; q < 18; q++) gL[q] = 0.0;
-        double ll = 0.0;
+// Output slots of one energy's gradient row: [0] LL, [1..6] theta12, theta13,
+// theta23, dCP, dm12sq, dm23sq, [7 + r] density of the caller's row r.
+constexpr int kLLOscOut = 7;
+
+// Block e, thread l < nl: layer l of energy e.  The thread sums the warps'
+// partials of its layer, re-solves the layer's eigen-problem in FP64, takes
+// the adjoint of its eigenvectors from the two overlaps it enters
+// (T_{l-1} = V_l^T V_{l-1} and T_l = V_{l+1}^T V_l, neighbours through shared
+// memory) and back-propagates through the eigen-decomposition to the
+// parameters.  The rows of the body map one-to-one to layers 1..nl-1, so each
+// density slot has a single writer; the oscillation parameters are summed
+// over the block in a fixed order.
+__global__ void __launch_bounds__(96) ll_layer_kernel(LLArgs a) {
+    __shared__ double sV[kMaxRows + 1][9];
+    __shared__ double sT[kMaxRows + 1][9];
+    __shared__ double sL[kLLPerE];
+    __shared__ double sRed[3][kLLOscOut];
+    const int e = blockIdx.x, l = threadIdx.x, nl = a.nl;
+    const OscParams& o = *a.osc;
+    const double E = a.energies[e];
+    double gT[9], gK0 = 0.0, gK1 = 0.0, m[3], V[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) gT[q] = 0.0;
+    if (l < nl) {
         for (int cc = 0; cc < a.n_cchunk; cc++) {
-            const double* pl = a.part_l + ((size_t)cc * a.n_en + e) * a.nl * kLLPerL;
-            for (int l = 0; l < a.nl; l++) {
-                for (int q = 0; q < 9; q++) gT[l][q] += pl[l * kLLPerL + q];
-                gK[l][0] += pl[l * kLLPerL + 9];
-                gK[l][1] += pl[l * kLLPerL + 10];
-            }
-            const double* pe = a.part_e + ((size_t)cc * a.n_en + e) * kLLPerE;
-            for (int q = 0; q < 18; q++) gL[q] += pe[q];
-            ll += pe[18];
+            const double* pl = a.part_l + (((size_t)cc * a.n_en + e) * nl + l) * kLLPerL;
+#pragma unroll
+            for (int q = 0; q < 9; q++) gT[q] += pl[q];
+            gK0 += pl[9];
+            gK1 += pl[10];
         }
-        grad[0] += ll;
-        // recompute every layer's eigen-decomposition and back-propagate
+        layer_eigen(o, E, a.rhoye[l], m, V);
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            sV[l][q] = V[q];
+            sT[l][q] = gT[q];
+        }
+    }
+    if (l < kLLPerE) {
+        double v = 0.0;
+        for (int cc = 0; cc < a.n_cchunk; cc++) v += a.part_e[((size_t)cc * a.n_en + e) * kLLPerE + l];
+        sL[l] = v;
+    }
+    __syncthreads();
+
+    double acc[kLLOscOut];
+#pragma unroll
+    for (int q = 0; q < kLLOscOut; q++) acc[q] = 0.0;
+    const int np = 6 + a.n_rows;
+    double* grow = a.part_g + (size_t)e * (1 + np);
+    if (l < nl) {
         const double s23 = o.s23, c23 = o.c23, sd = o.sd, cd = o.cd;
-        double gV[kMaxRows + 1][9];
-        double Vs[kMaxRows + 1][9], ms[kMaxRows + 1][3];
-        for (int l = 0; l < a.nl; l++) {
-            layer_eigen(o, E, a.rhoye[l], ms[l], Vs[l]);
-            for (int q = 0; q < 9; q++) gV[l][q] = 0.0;
-        }
-        // T_l = V_{l+1}^T V_l
-        for (int l = 0; l + 1 < a.nl; l++)
+        double gV[9];
+#pragma unroll
+        for (int q = 0; q < 9; q++) gV[q] = 0.0;
+        // T_l = V_{l+1}^T V_l: dT_l[i][j] / dV_l[r][j] = V_{l+1}[r][i]
+        if (l + 1 < nl) {
+#pragma unroll
             for (int i = 0; i < 3; i++)
-                for (int j = 0; j < 3; j++) {
-                    const double t = gT[l][3 * i + j];
-                    for (int r = 0; r < 3; r++) {
-                        gV[l + 1][3 * r + i] += t * Vs[l][3 * r + j];
-                        gV[l][3 * r + j] += t * Vs[l + 1][3 * r + i];
-                    }
-                }
-        // Lambda' from V_1: row 0 = V_1[0][k]; row 1 = c23 V_1[1][k] + s23 e^{i d} V_1[2][k]
-        double gth23 = 0.0, gdcp = 0.0;
-        for (int k = 0; k < 3; k++) {
-            const double gre = gL[3 + 2 * k], gim = gL[4 + 2 * k];
-            gV[1][k] += gL[k];
-            gV[1][3 + k] += c23 * gre;
-            gV[1][6 + k] += s23 * (gre * cd + gim * sd);
-            const double v1 = Vs[1][3 + k], v2 = Vs[1][6 + k];
-            // d/dtheta23: -s23 v1 + c23 e^{id} v2 ; d/ddcp: i s23 e^{id} v2
-            gth23 += gre * (-s23 * v1 + c23 * cd * v2) + gim * (c23 * sd * v2);
-            gdcp += gre * (-s23 * sd * v2) + gim * (s23 * cd * v2);
+#pragma unroll
+                for (int j = 0; j < 3; j++)
+#pragma unroll
+                    for (int r = 0; r < 3; r++) gV[3 * r + j] += sT[l][3 * i + j] * sV[l + 1][3 * r + i];
         }
-        // Gamma' from V_0: column 0 = V_0[0][k]; column 1 = c23 V_0[1][k] + s23 e^{-i d} V_0[2][k]
-        for (int k = 0; k < 3; k++) {
-            const double gre = gL[12 + 2 * k], gim = gL[13 + 2 * k];
-            gV[0][k] += gL[9 + k];
-            gV[0][3 + k] += c23 * gre;
-            gV[0][6 + k] += s23 * (gre * cd - gim * sd);
-            const double v1 = Vs[0][3 + k], v2 = Vs[0][6 + k];
-            gth23 += gre * (-s23 * v1 + c23 * cd * v2) + gim * (-c23 * sd * v2);
-            gdcp += gre * (-s23 * sd * v2) + gim * (-s23 * cd * v2);
+        // T_{l-1} = V_l^T V_{l-1}: dT_{l-1}[i][j] / dV_l[r][i] = V_{l-1}[r][j]
+        if (l >= 1) {
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int j = 0; j < 3; j++)
+#pragma unroll
+                    for (int r = 0; r < 3; r++) gV[3 * r + i] += sT[l - 1][3 * i + j] * sV[l - 1][3 * r + j];
         }
-        // eigen back-propagation per layer, then H_l = O diag(0, d1, d2) O^T - fac_l e0 e0^T
-        double gth12 = 0.0, gth13 = 0.0, gd1 = 0.0, gd2 = 0.0;
-        // O and its derivatives from the stored O matrix: O = R13 R12
+        if (l == 1) {
+            // Lambda' from V_1: row 0 = V_1[0][k]; row 1 = c23 V_1[1][k] + s23 e^{i d} V_1[2][k]
+            for (int k = 0; k < 3; k++) {
+                const double gre = sL[3 + 2 * k], gim = sL[4 + 2 * k];
+                gV[k] += sL[k];
+                gV[3 + k] += c23 * gre;
+                gV[6 + k] += s23 * (gre * cd + gim * sd);
+                const double v1 = V[3 + k], v2 = V[6 + k];
+                // d/dtheta23: -s23 v1 + c23 e^{id} v2 ; d/ddcp: i s23 e^{id} v2
+                acc[3] += gre * (-s23 * v1 + c23 * cd * v2) + gim * (c23 * sd * v2);
+                acc[4] += gre * (-s23 * sd * v2) + gim * (s23 * cd * v2);
+            }
+        }
+        if (l == 0) {
+            // Gamma' from V_0: column 0 = V_0[0][k]; column 1 = c23 V_0[1][k] + s23 e^{-i d} V_0[2][k]
+            for (int k = 0; k < 3; k++) {
+                const double gre = sL[12 + 2 * k], gim = sL[13 + 2 * k];
+                gV[k] += sL[9 + k];
+                gV[3 + k] += c23 * gre;
+                gV[6 + k] += s23 * (gre * cd - gim * sd);
+                const double v1 = V[3 + k], v2 = V[6 + k];
+                acc[3] += gre * (-s23 * v1 + c23 * cd * v2) + gim * (-c23 * sd * v2);
+                acc[4] += gre * (-s23 * sd * v2) + gim * (-s23 * cd * v2);
+            }
+            acc[0] = sL[18];
+        }
+        // eigen back-propagation; H_l = O diag(0, d1, d2) O^T - fac_l e0 e0^T.
+        // O = R13 R12 and its derivatives from the stored O matrix.
         const double* O = o.o;
         const double c13 = O[8], s13 = O[2];
         const double c12 = (c13 != 0.0) ? O[0] / c13 : O[4];
         const double sn12 = -O[3];
         const double dO12[9] = {-c13 * sn12, c13 * c12, 0.0, -c12, -sn12, 0.0, s13 * sn12, -s13 * c12, 0.0};
         const double dO13[9] = {-s13 * c12, -s13 * sn12, c13, 0.0, 0.0, 0.0, -c13 * c12, -c13 * sn12, -s13};
-        for (int l = 0; l < a.nl; l++) {
-            const double* V = Vs[l];
-            const double* m = ms[l];
-            // dLL/dm_k from the phase rates kappa_k = -LoE (m_k - m_0) / (2 pi E), k = 1, 2
-            const double f = -kLoEfac / (kTwoPi * E);
-            double gm[3] = {-(gK[l][0] + gK[l][1]) * f, gK[l][0] * f, gK[l][1] * f};
-            // gH = sum_k gm_k v_k v_k^T + sum_{k != j} (v_j . gv_k) / (m_k - m_j) v_j v_k^T
-            double W[3][3];  // W[j][k] = coefficient of v_j v_k^T
-            for (int j = 0; j < 3; j++)
-                for (int k = 0; k < 3; k++) {
-                    if (j == k) {
-                        W[j][k] = gm[k];
-                    } else {
-                        double dot = 0.0;
-                        for (int r = 0; r < 3; r++) dot += V[3 * r + j] * gV[l][3 * r + k];
-                        const double gap = m[k] - m[j];
-                        W[j][k] = (gap != 0.0) ? dot / gap : 0.0;
-                    }
+        // dLL/dm_k from the phase rates kappa_k = -LoE (m_k - m_0) / (2 pi E), k = 1, 2
+        const double f = -kLoEfac / (kTwoPi * E);
+        const double gm[3] = {-(gK0 + gK1) * f, gK0 * f, gK1 * f};
+        // gH = sum_k gm_k v_k v_k^T + sum_{k != j} (v_j . gv_k) / (m_k - m_j) v_j v_k^T
+        double W[3][3];  // W[j][k] = coefficient of v_j v_k^T
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                if (j == k) {
+                    W[j][k] = gm[k];
+                } else {
+                    double dot = 0.0;
+#pragma unroll
+                    for (int r = 0; r < 3; r++) dot += V[3 * r + j] * gV[3 * r + k];
+                    const double gap = m[k] - m[j];
+                    W[j][k] = (gap != 0.0) ? dot / gap : 0.0;
                 }
-            double gH[3][3];
-            for (int p = 0; p < 3; p++)
-                for (int q = 0; q < 3; q++) {
-                    double s = 0.0;
-                    for (int j = 0; j < 3; j++)
-                        for (int k = 0; k < 3; k++) s += W[j][k] * V[3 * p + j] * V[3 * q + k];
-                    gH[p][q] = s;
-                }
-            // symmetric part (H is symmetric)
-            for (int p = 0; p < 3; p++)
-                for (int q = p + 1; q < 3; q++) {
-                    const double s = 0.5 * (gH[p][q] + gH[q][p]);
-                    gH[p][q] = gH[q][p] = s;
-                }
-            // d1, d2: o_1^T gH o_1, o_2^T gH o_2
-            for (int p = 0; p < 3; p++)
-                for (int q = 0; q < 3; q++) {
-                    gd1 += gH[p][q] * O[3 * p + 1] * O[3 * q + 1];
-                    gd2 += gH[p][q] * O[3 * p + 2] * O[3 * q + 2];
-                }
-            // theta12, theta13: 2 tr(gH O D dO^T)
-            const double dd[3] = {0.0, o.d1, o.d2};
-            for (int p = 0; p < 3; p++)
-                for (int q = 0; q < 3; q++)
-                    for (int k = 1; k < 3; k++) {
-                        gth12 += 2.0 * gH[p][q] * O[3 * p + k] * dd[k] * dO12[3 * q + k];
-                        gth13 += 2.0 * gH[p][q] * O[3 * p + k] * dd[k] * dO13[3 * q + k];
-                    }
-            // densities: H[0][0] -= fac, fac = sgn GF E rho Ye
-            if (l >= 1) {
-                const int row = a.layer_row[l];
-                const double sgn = a.anti ? 1.0 : -1.0;
-                grad[1 + 6 + row] += -gH[0][0] * sgn * kGF * E * a.ye_layer[l];
             }
-        }
-        grad[1] += gth12;
-        grad[2] += gth13;
-        grad[3] += gth23;
-        grad[4] += gdcp;
+        double gH[3][3];
+#pragma unroll
+        for (int p = 0; p < 3; p++)
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+                double s = 0.0;
+#pragma unroll
+                for (int j = 0; j < 3; j++)
+#pragma unroll
+                    for (int k = 0; k < 3; k++) s += W[j][k] * V[3 * p + j] * V[3 * q + k];
+                gH[p][q] = s;
+            }
+#pragma unroll
+        for (int p = 0; p < 3; p++)
+#pragma unroll
+            for (int q = p + 1; q < 3; q++) {
+                const double s = 0.5 * (gH[p][q] + gH[q][p]);
+                gH[p][q] = gH[q][p] = s;
+            }
+        double gd1 = 0.0, gd2 = 0.0, gth12 = 0.0, gth13 = 0.0;
+        const double dd[3] = {0.0, o.d1, o.d2};
+#pragma unroll
+        for (int p = 0; p < 3; p++)
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+                // d1, d2: o_1^T gH o_1, o_2^T gH o_2
+                gd1 += gH[p][q] * O[3 * p + 1] * O[3 * q + 1];
+                gd2 += gH[p][q] * O[3 * p + 2] * O[3 * q + 2];
+                // theta12, theta13: 2 tr(gH O D dO^T)
+#pragma unroll
+                for (int k = 1; k < 3; k++) {
+                    gth12 += 2.0 * gH[p][q] * O[3 * p + k] * dd[k] * dO12[3 * q + k];
+                    gth13 += 2.0 * gH[p][q] * O[3 * p + k] * dd[k] * dO13[3 * q + k];
+                }
+            }
+        acc[1] = gth12;
+        acc[2] = gth13;
         // d1 = dm12sq, d2 = dm12sq + dm23sq
-        grad[5] += gd1 + gd2;
-        grad[6] += gd2;
-    }
-    // fixed-order block reduction of each output
-    for (int q = 0; q <= np; q++) {
-        s_acc[threadIdx.x] = grad[q];
-        __syncthreads();
-        for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-            if ((int)threadIdx.x < s) s_acc[threadIdx.x] += s_acc[threadIdx.x + s];
-            __syncthreads();
+        acc[5] = gd1 + gd2;
+        acc[6] = gd2;
+        // densities: H[0][0] -= fac, fac = sgn GF E rho Ye
+        if (l >= 1) {
+            const double sgn = a.anti ? 1.0 : -1.0;
+            grow[1 + 6 + a.layer_row[l]] = -gH[0][0] * sgn * kGF * E * a.ye_layer[l];
         }
-        if (threadIdx.x == 0) a.out[q] = s_acc[0];
-        __syncthreads();
+    }
+    // fixed-order block sum of the oscillation slots
+    const int w = l >> 5, lane = l & 31;
+#pragma unroll
+    for (int q = 0; q < kLLOscOut; q++) {
+        const double v = warp_sum(acc[q]);
+        if (lane == 0) sRed[w][q] = v;
+    }
+    __syncthreads();
+    if (l < kLLOscOut) {
+        double v = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) v += sRed[i][l];
+        grow[l] = v;
+    }
+}
+
+// Warp w sums output slot q = w, w + nwarps, ... over energies: lanes stride
+// the energies, then a butterfly; the order is fixed, the sum deterministic.
+__global__ void __launch_bounds__(256) ll_sum_kernel(LLArgs a) {
+    const int np1 = 7 + a.n_rows;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int q = w; q < np1; q += nw) {
+        double v = 0.0;
+        for (int e = lane; e < a.n_en; e += 32) v += a.part_g[(size_t)e * np1 + q];
+        v = warp_sum(v);
+        if (lane == 0) a.out[q] = v;
     }
 }
 
@@ -684,6 +731,7 @@ struct cp3_loglik {
     // device
     double *d_en = nullptr, *d_cos = nullptr, *d_radii = nullptr, *d_fe = nullptr, *d_fm = nullptr, *d_counts = nullptr;
     double *d_tab = nullptr, *d_pe = nullptr, *d_len = nullptr, *d_pl = nullptr, *d_pee = nullptr, *d_out = nullptr;
+    double* d_pg = nullptr;
     double *d_rhoye = nullptr, *d_yel = nullptr;
     int *d_maxl = nullptr, *d_row = nullptr;
     cp3::OscParams* d_osc = nullptr;
@@ -703,11 +751,11 @@ void ll_free(cp3_loglik* L) {
     L->exec = nullptr;
     L->graph = nullptr;
     void* ptrs[] = {L->d_en, L->d_cos, L->d_radii, L->d_fe, L->d_fm, L->d_counts, L->d_tab, L->d_pe, L->d_len,
-                    L->d_pl, L->d_pee, L->d_out, L->d_rhoye, L->d_yel, L->d_maxl, L->d_row, L->d_osc};
+                    L->d_pl, L->d_pee, L->d_out, L->d_pg, L->d_rhoye, L->d_yel, L->d_maxl, L->d_row, L->d_osc};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     L->d_en = L->d_cos = L->d_radii = L->d_fe = L->d_fm = L->d_counts = nullptr;
-    L->d_tab = L->d_pe = L->d_len = L->d_pl = L->d_pee = L->d_out = L->d_rhoye = L->d_yel = nullptr;
+    L->d_tab = L->d_pe = L->d_len = L->d_pl = L->d_pee = L->d_out = L->d_pg = L->d_rhoye = L->d_yel = nullptr;
     L->d_maxl = L->d_row = nullptr;
     L->d_osc = nullptr;
 }
@@ -746,6 +794,7 @@ cp3::LLArgs ll_args(cp3_loglik* L, int type) {
     a.len = L->d_len;
     a.part_l = L->d_pl;
     a.part_e = L->d_pee;
+    a.part_g = L->d_pg;
     a.out = L->d_out;
     a.layer_row = L->d_row;
     a.n_rows = L->n_rows;
@@ -782,7 +831,8 @@ int ll_setup(cp3_loglik* L, int type) {
     const size_t pee = (size_t)L->n_cchunk * L->n_en * cp3::kLLPerE;
     if ((e = cudaMalloc(&L->d_tab, tab * 8)) || (e = cudaMalloc(&L->d_pe, pe * 8)) || (e = cudaMalloc(&L->d_len, len * 8)) ||
         (e = cudaMalloc(&L->d_pl, pl * 8)) || (e = cudaMalloc(&L->d_pee, pee * 8)) ||
-        (e = cudaMalloc(&L->d_out, (cp3::kLLMaxParams + 1) * 8)) || (e = cudaMalloc(&L->d_rhoye, (cp3::kMaxRows + 1) * 8)) ||
+        (e = cudaMalloc(&L->d_out, (cp3::kLLMaxParams + 1) * 8)) ||
+        (e = cudaMalloc(&L->d_pg, (size_t)L->n_en * (cp3::kLLMaxParams + 1) * 8)) || (e = cudaMalloc(&L->d_rhoye, (cp3::kMaxRows + 1) * 8)) ||
         (e = cudaMalloc((void**)&L->d_osc, sizeof(cp3::OscParams))))
         return lcuda(e, "cudaMalloc(loglik)");
     // capture
@@ -809,7 +859,11 @@ int ll_setup(cp3_loglik* L, int type) {
         e = cudaGetLastError();
     }
     if (!e) {
-        cp3::ll_reduce_kernel<<<1, 256, 0, cs>>>(a);
+        cp3::ll_layer_kernel<<<L->n_en, (L->nl + 31) / 32 * 32, 0, cs>>>(a);
+        e = cudaGetLastError();
+    }
+    if (!e) {
+        cp3::ll_sum_kernel<<<1, 256, 0, cs>>>(a);
         e = cudaGetLastError();
     }
     if (!e) e = cudaMemcpyAsync(L->h_out, L->d_out, sizeof(double) * (7 + L->n_rows), cudaMemcpyDeviceToHost, cs);

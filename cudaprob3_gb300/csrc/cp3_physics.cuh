@@ -19,29 +19,112 @@ namespace cp3 {
 
 // Eigen-decomposition of the real symmetric 2E*H_r of one layer.
 //   m[k]       eigenvalues in eV^2 (order of the trigonometric roots)
-//   V[3*i+k]   component i of the unit eigenvector of m[k]
+//   V[3*i+k]   component i of the unit eigenvector of m[k]; det V = +1
 // `rhoye` is rho*Ye in g/cm^3 (the reference passes rho*0.5, physics.hpp:651).
+//
+// The roots are those of Barger Eqs. 21-22 (physics.hpp:284-324): the cubic
+// x^3 + a x^2 + b x + g with the reference's coefficients.  The trigonometric
+// angle and its cosines are taken in FP32 (a first guess good to ~1e-7), then
+// two FP64 Newton steps on the cubic bring each root to FP64 accuracy; this
+// replaces the FP64 acos and cos of the reference and is also accurate where
+// acos loses digits (arg near +-1).  Eigenvectors: the largest column of the
+// Lagrange projector (H - m_a)(H - m_b) for m_0 and m_1, and v_2 = v_0 x v_1,
+// which makes every basis right-handed (the propagation kernels rely on
+// det T_l = +1 for T_l = V_{l+1}^T V_l).
+CP3_HD double cubic_newton(double x, double a, double b, double g) {
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        const double p = fma(fma(x + a, x, b), x, g);
+        const double dp = fma(fma(3.0, x, 2.0 * a), x, b);
+        if (dp != 0.0) x -= p / dp;
+    }
+    return x;
+}
+
+CP3_HD void eigvec_of(const double H[9], double m, double ma, double mb, double v[3]) {
+    // columns of N = (H - ma)(H - mb) are parallel to the eigenvector of m;
+    // take the one with the largest diagonal entry
+    const double a0 = H[0] - ma, a4 = H[4] - ma, a8 = H[8] - ma;
+    const double b0 = H[0] - mb, b4 = H[4] - mb, b8 = H[8] - mb;
+    const double n00 = a0 * b0 + H[1] * H[3] + H[2] * H[6];
+    const double n11 = H[3] * H[1] + a4 * b4 + H[5] * H[7];
+    const double n22 = H[6] * H[2] + H[7] * H[5] + a8 * b8;
+    double c0, c1, c2;
+    if (fabs(n00) >= fabs(n11) && fabs(n00) >= fabs(n22)) {
+        c0 = n00;
+        c1 = H[3] * b0 + a4 * H[3] + H[5] * H[6];
+        c2 = H[6] * b0 + H[7] * H[3] + a8 * H[6];
+    } else if (fabs(n11) >= fabs(n22)) {
+        c0 = a0 * H[1] + H[1] * b4 + H[2] * H[7];
+        c1 = n11;
+        c2 = H[6] * H[1] + H[7] * b4 + a8 * H[7];
+    } else {
+        c0 = a0 * H[2] + H[1] * H[5] + H[2] * b8;
+        c1 = H[3] * H[2] + a4 * H[5] + H[5] * b8;
+        c2 = n22;
+    }
+    const double nrm = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+    double inv = (nrm > 0.0) ? 1.0 / nrm : 0.0;
+    // deterministic sign: largest component positive
+    double big = c0;
+    if (fabs(c1) > fabs(big)) big = c1;
+    if (fabs(c2) > fabs(big)) big = c2;
+    if (big < 0.0) inv = -inv;
+    v[0] = c0 * inv;
+    v[1] = c1 * inv;
+    v[2] = c2 * inv;
+}
+
 CP3_HD void layer_eigen(const OscParams& p, double E, double rhoye, double m[3], double V[9]) {
     // physics.hpp:277-295: matter term and the cubic's coefficients
     const double fac = p.anti ? kGF * E * rhoye : -(kGF * E * rhoye);
     const double a = fac + p.dm01 + p.dm02;
     const double b = p.dm01 * p.dm02 + fac * (p.dm01 * (1.0 - p.u01) + p.dm02 * (1.0 - p.u02));
     const double g = fac * p.dm01 * p.dm02 * p.u00;
-    // physics.hpp:298-324: trigonometric roots
+    // physics.hpp:298-324: trigonometric roots (first guess), then Newton
     double tmp = a * a - 3.0 * b;
     if (tmp < 0.0) tmp = 0.0;
     const double sq = sqrt(tmp);
     double arg = (2.0 * a * a * a - 9.0 * a * b + 27.0 * g) / (2.0 * sq * tmp);
     if (!(fabs(arg) <= 1.0)) arg = (arg > 0.0) ? 1.0 : -1.0;
-    const double th = acos(arg) / 3.0;
-    double s, c;
-    sincos(th, &s, &c);
+    const float th = acosf((float)arg) * (1.0f / 3.0f);
+    float sf, cf;
+    sincosf(th, &sf, &cf);
+    const double c = cf, s = sf;
     const double h = 0.86602540378443864676;  // sin(2pi/3)
     const double amp = -(2.0 / 3.0) * sq;
     const double sh = -a / 3.0;
-    m[0] = amp * c + sh;                       // cos(th)
-    m[1] = amp * (-0.5 * c + h * s) + sh;      // cos(th - 2pi/3)
-    m[2] = amp * (-0.5 * c - h * s) + sh;      // cos(th + 2pi/3)
+    {
+    double q[3];
+    q[0] = amp * c + sh;                   // cos(th)
+    q[1] = amp * (-0.5 * c + h * s) + sh;  // cos(th - 2pi/3)
+    q[2] = amp * (-0.5 * c - h * s) + sh;  // cos(th + 2pi/3)
+    // Newton converges fast only on a well separated root, and the degeneracy
+    // break leaves a pair 5e-9 eV^2 apart: refine the most isolated root i,
+    // then take the other two from the deflated quadratic x^2 - S x + P with
+    // S = -a - m_i and P = -g/m_i (or b - m_i S when m_i is not the largest).
+    const double e0 = fmin(fabs(q[0] - q[1]), fabs(q[0] - q[2]));
+    const double e1 = fmin(fabs(q[1] - q[0]), fabs(q[1] - q[2]));
+    const double e2 = fmin(fabs(q[2] - q[0]), fabs(q[2] - q[1]));
+    const int ri = (e0 >= e1 && e0 >= e2) ? 0 : (e1 >= e2) ? 1 : 2;
+    const int rj = (ri + 1) % 3, rk = (ri + 2) % 3;
+    const double qi = (ri == 0) ? q[0] : (ri == 1) ? q[1] : q[2];
+    const double qj = (rj == 0) ? q[0] : (rj == 1) ? q[1] : q[2];
+    const double qk = (rk == 0) ? q[0] : (rk == 1) ? q[1] : q[2];
+    const double mi = cubic_newton(qi, a, b, g);
+    const double S = -a - mi;
+    const double P = (fabs(mi) >= fabs(qj) && fabs(mi) >= fabs(qk) && mi != 0.0) ? -g / mi : b - mi * S;
+    double disc = S * S - 4.0 * P;
+    if (disc < 0.0) disc = 0.0;
+    const double big = 0.5 * (S + copysign(sqrt(disc), S));
+    const double small = (big != 0.0) ? P / big : 0.0;
+    const double hi = fmax(big, small), lo = fmin(big, small);
+    const double mj = (qj >= qk) ? hi : lo;
+    const double mk = (qj >= qk) ? lo : hi;
+    m[0] = (ri == 0) ? mi : (rj == 0) ? mj : mk;
+    m[1] = (ri == 1) ? mi : (rj == 1) ? mj : mk;
+    m[2] = (ri == 2) ? mi : (rj == 2) ? mj : mk;
+    }
 
     // H_r = O diag(0, d1, d2) O^T - fac e0 e0^T
     double H[9];
@@ -52,48 +135,46 @@ CP3_HD void layer_eigen(const OscParams& p, double E, double rhoye, double m[3],
             H[3 * i + j] = p.d1 * p.o[3 * i + 1] * p.o[3 * j + 1] + p.d2 * p.o[3 * i + 2] * p.o[3 * j + 2];
     H[0] -= fac;
 
-    // Eigenvector of m[k]: the largest column of (H - m_a)(H - m_b).
+    // The most isolated eigenvalue i gets its projector column; the next most
+    // isolated j too, made exactly orthogonal to v_i; the third is their cross
+    // product.  A near-degenerate pair (the degeneracy break of
+    // propagator.hpp:226-248) then still yields an orthonormal basis.
+    const double g0 = fmin(fabs(m[0] - m[1]), fabs(m[0] - m[2]));
+    const double g1 = fmin(fabs(m[1] - m[0]), fabs(m[1] - m[2]));
+    const double g2 = fmin(fabs(m[2] - m[0]), fabs(m[2] - m[1]));
+    int i = 0;
+    if (g1 > g0) i = 1;
+    if (g2 > (i == 0 ? g0 : g1)) i = 2;
+    const int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+    const double gi1 = (i1 == 0) ? g0 : (i1 == 1) ? g1 : g2;
+    const double gi2 = (i2 == 0) ? g0 : (i2 == 1) ? g1 : g2;
+    const bool cyc = gi1 >= gi2;  // j = i+1, k = i+2 (cyclic) or j = i+2, k = i+1
+    const int j = cyc ? i1 : i2;
+    const double mi = (i == 0) ? m[0] : (i == 1) ? m[1] : m[2];
+    const double mj = (j == 0) ? m[0] : (j == 1) ? m[1] : m[2];
+    const int k = 3 - i - j;
+    const double mk = (k == 0) ? m[0] : (k == 1) ? m[1] : m[2];
+    double vi[3], vj[3], vk[3];
+    eigvec_of(H, mi, mj, mk, vi);
+    eigvec_of(H, mj, mk, mi, vj);
+    const double d = vj[0] * vi[0] + vj[1] * vi[1] + vj[2] * vi[2];
+    vj[0] -= d * vi[0];
+    vj[1] -= d * vi[1];
+    vj[2] -= d * vi[2];
+    const double nj = sqrt(vj[0] * vj[0] + vj[1] * vj[1] + vj[2] * vj[2]);
+    const double rj = (nj > 0.0) ? 1.0 / nj : 0.0;
+    vj[0] *= rj;
+    vj[1] *= rj;
+    vj[2] *= rj;
+    // (i, j, k) cyclic: v_k = v_i x v_j; otherwise v_k = v_j x v_i
+    const double sgn = cyc ? 1.0 : -1.0;
+    vk[0] = sgn * (vi[1] * vj[2] - vi[2] * vj[1]);
+    vk[1] = sgn * (vi[2] * vj[0] - vi[0] * vj[2]);
+    vk[2] = sgn * (vi[0] * vj[1] - vi[1] * vj[0]);
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
-        const double ma = m[(k + 1) % 3], mb = m[(k + 2) % 3];
-        double A[9], B[9];
+    for (int r = 0; r < 3; r++) {
 #pragma unroll
-        for (int i = 0; i < 9; i++) {
-            A[i] = H[i];
-            B[i] = H[i];
-        }
-        A[0] -= ma; A[4] -= ma; A[8] -= ma;
-        B[0] -= mb; B[4] -= mb; B[8] -= mb;
-        double N[9];
-#pragma unroll
-        for (int i = 0; i < 3; i++)
-#pragma unroll
-            for (int j = 0; j < 3; j++)
-                N[3 * i + j] = A[3 * i] * B[j] + A[3 * i + 1] * B[3 + j] + A[3 * i + 2] * B[6 + j];
-        int col = 0;
-        double best = fabs(N[0]);
-        if (fabs(N[4]) > best) { best = fabs(N[4]); col = 1; }
-        if (fabs(N[8]) > best) { best = fabs(N[8]); col = 2; }
-        double v0 = N[col], v1 = N[3 + col], v2 = N[6 + col];
-        const double nrm = sqrt(v0 * v0 + v1 * v1 + v2 * v2);
-        double inv = (nrm > 0.0) ? 1.0 / nrm : 0.0;
-        // deterministic sign: largest component positive
-        double big = v0;
-        if (fabs(v1) > fabs(big)) big = v1;
-        if (fabs(v2) > fabs(big)) big = v2;
-        if (big < 0.0) inv = -inv;
-        V[k] = v0 * inv;
-        V[3 + k] = v1 * inv;
-        V[6 + k] = v2 * inv;
-    }
-    // right-handed basis (det V = +1): every overlap T_l = V_{l+1}^T V_l is then a
-    // rotation, which the propagation kernels rely on to rebuild a column
-    const double det = V[0] * (V[4] * V[8] - V[5] * V[7]) - V[1] * (V[3] * V[8] - V[5] * V[6]) +
-                       V[2] * (V[3] * V[7] - V[4] * V[6]);
-    if (det < 0.0) {
-        V[2] = -V[2];
-        V[5] = -V[5];
-        V[8] = -V[8];
+        for (int c = 0; c < 3; c++) V[3 * r + c] = (c == i) ? vi[r] : (c == j) ? vj[r] : vk[r];
     }
 }
 
