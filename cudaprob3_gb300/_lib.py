@@ -49,6 +49,7 @@ SIGNATURES = [
     ("cp3_result_bytes", _I, [_P, ctypes.POINTER(_SZ)]),
     ("cp3_copy_results_to_host", _I, [_P, _P, _SZ]),
     ("cp3_set_result_buffer", _I, [_P, _P, _SZ]),
+    ("cp3_set_host_result_buffer", _I, [_P, _P, _SZ]),
     ("cp3_set_stream", _I, [_P, _P]),
     ("cp3_last_launch_count", _I, [_P, _IP]),
     ("cp3_get_maxlayers", _I, [_P, _IP, _I]),

@@ -91,6 +91,7 @@ struct cp3_propagator {
     DevBuf<int4> d_ptab;
     void* ext_result = nullptr;
     size_t ext_bytes = 0;
+    void* ext_host = nullptr;  // caller page-locked host buffer behind ext_result (zero-copy)
     bool maxl_dirty = true, energy_dirty = true, cosine_dirty = true, density_dirty = true;
 
     // pinned host copy for getProbability (cudapropagator.cuh:73, 168-181)
@@ -363,6 +364,30 @@ int cp3_set_result_buffer(cp3_propagator* p, void* dptr, size_t bytes) {
         return fail(CP3_ERR_ARGUMENT, "set_result_buffer: buffer smaller than 9*n_cos*n_en elements");
     p->ext_result = dptr;
     p->ext_bytes = dptr ? bytes : 0;
+    p->ext_host = nullptr;
+    p->results_on_host = false;
+    return CP3_OK;
+}
+
+int cp3_set_host_result_buffer(cp3_propagator* p, void* host, size_t bytes) {
+    if (int rc = check(p)) return rc;
+    if (!host) return cp3_set_result_buffer(p, nullptr, 0);
+    if (bytes < p->result_bytes())
+        return fail(CP3_ERR_ARGUMENT, "set_host_result_buffer: buffer smaller than 9*n_cos*n_en elements");
+    DeviceGuard g(p->device);
+    // page-locked memory reports cudaMemoryTypeHost and its device alias;
+    // pageable memory reports cudaMemoryTypeUnregistered
+    cudaPointerAttributes at{};
+    cudaError_t e = cudaPointerGetAttributes(&at, host);
+    void* dptr = (e == cudaSuccess && at.type == cudaMemoryTypeHost) ? at.devicePointer : nullptr;
+    if (!dptr) {
+        cudaGetLastError();
+        return fail(CP3_ERR_ARGUMENT,
+                    "set_host_result_buffer: not page-locked host memory (use cudaHostAlloc or cudaHostRegister)");
+    }
+    p->ext_result = dptr;
+    p->ext_bytes = bytes;
+    p->ext_host = host;
     p->results_on_host = false;
     return CP3_OK;
 }
@@ -563,6 +588,16 @@ int cp3_get_probability(cp3_propagator* p, int ic, int ie, int t, double* out) {
     if (ic >= p->n_cos || ie >= p->n_en || ic < 0 || ie < 0)
         return fail(CP3_ERR_ARGUMENT, "CudaPropagatorSingle::getProbability. Invalid indices");
     if (t < 0 || t > 8) return fail(CP3_ERR_ARGUMENT, "getProbability: ProbType out of range");
+    if (p->ext_host) {
+        // the kernel stored the planes straight into the caller's host buffer
+        if (!p->results_on_host) {
+            if (int rc = cp3_wait_for_completion(p)) return rc;
+            p->results_on_host = true;
+        }
+        const size_t idx = (size_t)t * p->n_en * p->n_cos + (size_t)ic * p->n_en + ie;
+        *out = p->mixed ? (double)((const float*)p->ext_host)[idx] : ((const double*)p->ext_host)[idx];
+        return CP3_OK;
+    }
     if (!p->results_on_host) {
         DeviceGuard g(p->device);
         if (!p->h_result) {

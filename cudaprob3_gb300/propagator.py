@@ -170,6 +170,12 @@ class CudaPropagatorSingle:
     def set_result_buffer(self, device_ptr, nbytes):
         check(self._lib.cp3_set_result_buffer(self._h, ctypes.c_void_p(device_ptr), int(nbytes)))
 
+    def set_host_result_buffer(self, host_ptr, nbytes):
+        """Zero-copy host results into page-locked memory at `host_ptr`
+        (cudaHostAlloc / cudaHostRegister, e.g. a pinned torch tensor); 0
+        returns to the device buffer.  Pageable memory raises CP3Error."""
+        check(self._lib.cp3_set_host_result_buffer(self._h, ctypes.c_void_p(host_ptr), int(nbytes)))
+
     def set_stream(self, stream_handle):
         check(self._lib.cp3_set_stream(self._h, ctypes.c_void_p(stream_handle)))
 

@@ -125,6 +125,13 @@ public:
         out.resize((size_t)9 * this->n_cosines * this->n_energies);
         detail::check(cp3_copy_results_to_host(alive(), out.data(), out.size() * sizeof(FLOAT_T)));
     }
+    /// Zero-copy host results: `host` is page-locked (cudaHostAlloc or
+    /// cudaHostRegister) memory of >= 9 * n_cosines * n_energies elements; the
+    /// kernel stores the planes straight into it and getProbability reads it
+    /// without a copy.  nullptr returns to the device buffer.
+    void setHostResultBuffer(FLOAT_T* host, size_t elements) {
+        detail::check(cp3_set_host_result_buffer(alive(), host, elements * sizeof(FLOAT_T)));
+    }
     cp3_propagator* handle() { return h; }
 
 private:

@@ -130,6 +130,16 @@ int cp3_copy_results_to_host(cp3_propagator* p, void* dst, size_t bytes);
  * the next calculation on; NULL returns to the handle's own buffer. */
 int cp3_set_result_buffer(cp3_propagator* p, void* dptr, size_t bytes);
 
+/* Zero-copy host results (no reference counterpart: the reference copies
+ * d_result_list into its pinned resultList on the first getProbability after
+ * a calculation, cudapropagator.cuh:168-181 and 228-234).  `host` must be page-locked (cudaHostAlloc or
+ * cudaHostRegister) and hold >= cp3_result_bytes; from the next calculation on
+ * the kernel stores the planes straight into it over the host link, so the
+ * transfer overlaps the computation.  cp3_get_probability then reads it
+ * without a copy.  Pageable memory is rejected with CP3_ERR_ARGUMENT; NULL
+ * returns to the handle's own device buffer. */
+int cp3_set_host_result_buffer(cp3_propagator* p, void* host, size_t bytes);
+
 /* Run on a caller-owned cudaStream_t (NULL returns to the handle's own stream). */
 int cp3_set_stream(cp3_propagator* p, void* cuda_stream);
 

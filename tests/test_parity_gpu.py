@@ -186,6 +186,32 @@ def test_external_buffer_and_stream(gpu):
         p.set_stream(0)
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_host_result_buffer_zero_copy(gpu, precision):
+    """Kernel stores straight into page-locked host memory: same bits as the
+    device buffer, getProbability reads it, pageable memory is refused."""
+    torch = pytest.importorskip("torch")
+    c = G.linspace(-1, 0, 80)
+    e = G.logspace(0.1, 1000, 112)
+    dt = torch.float32 if precision == "mixed" else torch.float64
+    with make(gpu, precision, c, e, G.PREM_12.radii, G.PREM_12.rhos, G.PREM_12.ye, G.NOMINAL) as p:
+        p.calculateProbabilities(gpu.Antineutrino)
+        own = p.results()
+        host = torch.full((9, 80, 112), -1.0, dtype=dt).pin_memory()
+        p.set_host_result_buffer(host.data_ptr(), host.numel() * host.element_size())
+        p.calculateProbabilities(gpu.Antineutrino)
+        assert np.array_equal(host.numpy(), own)
+        assert p.getProbability(17, 33, gpu.ProbType.m_e) == float(own[3, 17, 33])
+        with pytest.raises(gpu.CP3Error):
+            p.set_host_result_buffer(host.data_ptr(), 16)
+        pageable = np.empty(9 * 80 * 112, dtype=own.dtype)
+        with pytest.raises(gpu.CP3Error, match="page-locked"):
+            p.set_host_result_buffer(pageable.ctypes.data, pageable.nbytes)
+        p.set_host_result_buffer(0, 0)
+        p.calculateProbabilities(gpu.Neutrino)
+        assert not np.array_equal(p.results(), own)
+
+
 def test_configs1_scale_mixed_vs_fp64(gpu):
     """4096 x 4096 grid, 0.1-1000 GeV, 11-shell body: the mixed kernel against
     the FP64 kernel on every pair (device-side comparison) and against the
