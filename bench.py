@@ -308,13 +308,10 @@ def run_ours(args, world, rank, local):
         hbm_peak, hbm_src = float(mp["hbm_gbs"]), "MEASURED_PEAKS.json (measured)"
     except (OSError, KeyError, ValueError):
         hbm_peak, hbm_src = 6800.0, "fallback 6.8 TB/s"
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "propagate_mixed_traffic.json")
-    if os.path.exists(tp):
-        try:
-            traffic = json.load(open(tp)).get("dram_bytes_per_launch_at_4096x4096")
-        except ValueError:
-            traffic = None
+    # DRAM bytes (read + write) of one propagate_kernel<mixed> launch at
+    # 4096 x 4096 from an ncu capture of that launch (dram__bytes_read.sum +
+    # dram__bytes_write.sum; summary in profiles/propagate_mixed_4096x4096_ncu.md)
+    traffic = 545_937_664 if (NC, NE) == (4096, 4096) else None
     roofline = {
         "bound": "fma-pipe (mad.wide.s32 integer MAC on the FMA-heavy pipe)",
         "achieved": madw / (prop_ms * 1e-3) / 1e12, "peak": peak_madw / 1e12, "unit": "Tops/s",
