@@ -42,6 +42,8 @@ constexpr int kLLTile = 32;          // energies per table tile of the likelihoo
 constexpr int kLLPerE = 19;          // per (warp, energy): Lambda' (9), Gamma' (9), LL
 constexpr int kLLPerL = 11;          // per (warp, energy, layer): T (9), kappa (2)
 constexpr int kLLMaxParams = 6 + kMaxRows;
+constexpr int kLLFWords = 13;        // float shadow per (energy, layer): T (9), kappa_1, kappa_2 as hi/lo
+constexpr int kLLEigWords = 12;      // per (energy, layer): V (9), m (3)
 
 // ------------------------------------------------------------ complex ----
 template <class T>
@@ -119,6 +121,12 @@ struct LLArgs {
     const int* layer_row;  // [nl]: caller's row of layer l (l >= 1), -1 for layer 0
     int n_rows;
     const double* ye_layer;  // [nl]
+    // FP64 eigen-pairs of every (energy, layer) for the reduction
+    double* eig;     // [n_en_pad][nl][12]
+    // float shadows of the tables for the mixed pair kernel (null for FP64)
+    float* tabf;     // tile-major [n_en_pad/32][nl][13][32]
+    float* pef;      // [18][n_en_pad]
+    float2* lenf;    // [n_cos][nl_pad], hi/lo
 };
 
 // ---------------------------------------------------------------- prep ----
@@ -134,14 +142,45 @@ __global__ void __launch_bounds__(256) ll_prep_kernel(LLArgs a) {
         double* vme = s_v + ((size_t)ey * nl + (l < nl ? l : 0)) * 9;
         if (live) {
             const double E = a.energies[e < a.n_en ? e : a.n_en - 1];
-            prep_energy_layer<false>(*a.osc, E, a.rhoye[l], l, e, g, vme);
+            double* ev = a.eig + ((size_t)e * nl + l) * kLLEigWords;
+            prep_energy_layer<false>(*a.osc, E, a.rhoye[l], l, e, g, vme, ev + 9);
+#pragma unroll
+            for (int q = 0; q < 9; q++) ev[q] = vme[q];
         }
         __syncthreads();
         if (live) prep_overlap<false>(l, e, g, vme);
+        if (a.tabf) {
+            // float shadow of this (energy, layer)'s words; thread l = 0 also
+            // converts the energy's Lambda' / Gamma' (written by l = 0 and 1)
+            __syncthreads();
+            if (live) {
+                const int tile = e / kLLTile, ln = e % kLLTile;
+                const double* t = a.tab + ((size_t)tile * nl + l) * kFp64Words * kLLTile + ln;
+                float* f = a.tabf + ((size_t)tile * nl + l) * kLLFWords * kLLTile + ln;
+#pragma unroll
+                for (int q = 0; q < 9; q++) f[q * kLLTile] = (float)t[q * kLLTile];
+#pragma unroll
+                for (int k = 0; k < 2; k++) {
+                    const double kd = t[(9 + k) * kLLTile];
+                    const float kh = (float)kd;
+                    f[(9 + 2 * k) * kLLTile] = kh;
+                    f[(10 + 2 * k) * kLLTile] = (float)(kd - (double)kh);
+                }
+                if (l == 0)
+                    for (int w = 0; w < 18; w++)
+                        a.pef[(size_t)w * a.n_en_pad + e] = (float)a.pe[(size_t)w * a.n_en_pad + e];
+            }
+        }
     } else {
         const int c = (blockIdx.x - nbE) * (blockDim.x * blockDim.y) + threadIdx.y * blockDim.x + threadIdx.x;
         if (c >= a.n_cos) return;
         prep_cosine<false>(a.cosines[c], a.maxl[c], a.radii, a.height_cm, c, g);
+        if (a.lenf)
+            for (int l = 0; l < a.nl_pad; l++) {
+                const double L = a.len[(size_t)c * a.nl_pad + l];
+                const float h = (float)L;
+                a.lenf[(size_t)c * a.nl_pad + l] = make_float2(h, (float)(L - (double)h));
+            }
     }
 }
 
@@ -162,22 +201,42 @@ struct LLTab {
     __device__ __forceinline__ double pe_w(int w) const { return pe[(size_t)w * n_en_pad + e]; }
 };
 
+// Table source of the pair kernel for energy e and cosine c: FP64 tables for
+// the FP64 kernel, their float shadows (kappa and lengths as hi/lo pairs) for
+// the mixed kernel, so that its loops hold no FP64 instruction.
 template <class R>
-struct Phase;
+struct LLSrc;
 template <>
-struct Phase<double> {
+struct LLSrc<double> {
+    LLTab tb;
+    const double* len;  // this cosine's [nl_pad]
+    __device__ __forceinline__ LLSrc(const LLArgs& a, int e, int c)
+        : tb{a.tab, a.pe, e, a.nl, a.n_en_pad}, len(a.len + (size_t)c * a.nl_pad) {}
+    __device__ __forceinline__ double T(int l, int i, int j) const { return tb.T(l, i, j); }
     // e^{i psi_k} of layer l, k = 1, 2 (table words kappa_1, kappa_2)
-    __device__ static Cx<double> get(const LLTab& t, int l, int k, const double* len) {
-        return phase_of(t.kap(l, k - 1), len[l]);
-    }
+    __device__ __forceinline__ Cx<double> D(int l, int k) const { return phase_of(tb.kap(l, k - 1), len[l]); }
+    __device__ __forceinline__ double L(int l) const { return len[l]; }
+    __device__ __forceinline__ double pe(int w) const { return tb.pe_w(w); }
 };
 template <>
-struct Phase<float> {
-    __device__ static Cx<float> get(const LLTab& t, int l, int k, const double* len) {
-        const double kd = t.kap(l, k - 1), Ld = len[l];
-        const float kh = (float)kd, Lh = (float)Ld;
-        return phase_of(make_float2(kh, (float)(kd - (double)kh)), make_float2(Lh, (float)(Ld - (double)Lh)));
+struct LLSrc<float> {
+    const float* f;      // this energy's column of layer 0 in the tile-major shadow
+    const float* pef;
+    const float2* len;
+    int e, n_en_pad;
+    __device__ __forceinline__ LLSrc(const LLArgs& a, int e_, int c)
+        : f(a.tabf + (size_t)(e_ / kLLTile) * a.nl * kLLFWords * kLLTile + e_ % kLLTile),
+          pef(a.pef),
+          len(a.lenf + (size_t)c * a.nl_pad),
+          e(e_),
+          n_en_pad(a.n_en_pad) {}
+    __device__ __forceinline__ float T(int l, int i, int j) const { return f[(l * kLLFWords + 3 * i + j) * kLLTile]; }
+    __device__ __forceinline__ Cx<float> D(int l, int k) const {
+        const float kh = f[(l * kLLFWords + 7 + 2 * k) * kLLTile], kl = f[(l * kLLFWords + 8 + 2 * k) * kLLTile];
+        return phase_of(make_float2(kh, kl), len[l]);
     }
+    __device__ __forceinline__ float L(int l) const { return len[l].x; }
+    __device__ __forceinline__ float pe(int w) const { return pef[(size_t)w * n_en_pad + e]; }
 };
 
 template <class R>
@@ -191,8 +250,7 @@ __global__ void __launch_bounds__(128) ll_pair_kernel(LLArgs a) {
     const bool valid = c < a.n_cos;
     const int M = valid ? a.maxl[c] : 0;
     const int Mw = __reduce_max_sync(0xffffffffu, M);
-    const LLTab tb{a.tab, a.pe, e, a.nl, a.n_en_pad};
-    const double* len = a.len + (size_t)(valid ? c : 0) * a.nl_pad;
+    const LLSrc<R> src(a, e, valid ? c : 0);
     const R twopi = (R)kTwoPi;
 
     // per-energy tables: Lambda' (row 0 real, row 1 complex), Gamma' (col 0 real, col 1 complex)
@@ -202,13 +260,13 @@ __global__ void __launch_bounds__(128) ll_pair_kernel(LLArgs a) {
     C Gb[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        La[k] = (R)tb.pe_w(k);
-        Lb[k] = C{(R)tb.pe_w(3 + 2 * k), (R)tb.pe_w(4 + 2 * k)};
-        Ga[k] = (R)tb.pe_w(9 + k);
-        Gb[k] = C{(R)tb.pe_w(12 + 2 * k), (R)tb.pe_w(13 + 2 * k)};
+        La[k] = src.pe(k);
+        Lb[k] = C{src.pe(3 + 2 * k), src.pe(4 + 2 * k)};
+        Ga[k] = src.pe(9 + k);
+        Gb[k] = C{src.pe(12 + 2 * k), src.pe(13 + 2 * k)};
     }
-    auto T = [&](int l, int i, int j) -> R { return (R)tb.T(l, i, j); };
-    auto D = [&](int l, int k) -> C { return Phase<R>::get(tb, l, k, len); };  // k = 1, 2
+    auto T = [&](int l, int i, int j) -> R { return src.T(l, i, j); };
+    auto D = [&](int l, int k) -> C { return src.D(l, k); };  // k = 1, 2
 
     // ---------------- forward
     C D0[3] = {C{1, 0}, D(0, 1), D(0, 2)};
@@ -397,7 +455,7 @@ __global__ void __launch_bounds__(128) ll_pair_kernel(LLArgs a) {
         if (l == M) {
             // D_M = diag(1, e^{i psi1}, e^{i psi2}): dLL/dkappa_k = 2 pi L * (-Im(conj(gD) D))
 #pragma unroll
-            for (int k = 1; k < 3; k++) tk[k - 1] = -twopi * (R)len[l] * cjmul(gDM[k], DM[k]).im;
+            for (int k = 1; k < 3; k++) tk[k - 1] = -twopi * src.L(l) * cjmul(gDM[k], DM[k]).im;
         } else if (l < M) {
             // Y_l = T_l U, U = D_l Y_{l-1}; un-multiply: U = T_l^T Y_l, Y_{l-1} = conj(D_l) U
             const C dl[3] = {C{1, 0}, D(l, 1), D(l, 2)};
@@ -430,24 +488,27 @@ __global__ void __launch_bounds__(128) ll_pair_kernel(LLArgs a) {
                         Y[k][j] = yp;
                         gY[k][j] = cjmul(dl[k], gU[k][j]);
                     }
-                    if (k > 0) tk[k - 1] = -twopi * (R)len[l] * cjmul(gd, dl[k]).im;
+                    if (k > 0) tk[k - 1] = -twopi * src.L(l) * cjmul(gd, dl[k]).im;
                 }
             } else {
                 // l = 1: Y_1 = T_1 D_1, so U = D_1 and gU holds the adjoint of D_1 on the diagonal
 #pragma unroll
-                for (int k = 1; k < 3; k++) tk[k - 1] = -twopi * (R)len[1] * cjmul(gU[k][k], dl[k]).im;
+                for (int k = 1; k < 3; k++) tk[k - 1] = -twopi * src.L(1) * cjmul(gU[k][k], dl[k]).im;
             }
         }
-        // warp reduction of this layer's 11 values (lanes with nothing to add give zeros)
+        // warp reduction of this layer's 11 values (lanes with nothing to add
+        // give zeros), in the kernel's precision: each term already carries
+        // that precision's rounding, a 5-level tree adds at most 5 ulp of the
+        // absolute sum
 #pragma unroll
         for (int q = 0; q < 9; q++) {
-            const double v = warp_sum((double)tT[q]);
-            if (lane == 0) pl[(size_t)l * kLLPerL + q] = v;
+            const R v = warp_sum(tT[q]);
+            if (lane == 0) pl[(size_t)l * kLLPerL + q] = (double)v;
         }
 #pragma unroll
         for (int k = 0; k < 2; k++) {
-            const double v = warp_sum((double)tk[k]);
-            if (lane == 0) pl[(size_t)l * kLLPerL + 9 + k] = v;
+            const R v = warp_sum(tk[k]);
+            if (lane == 0) pl[(size_t)l * kLLPerL + 9 + k] = (double)v;
         }
     }
     // layers above Mw are never crossed by this warp's cosines
@@ -458,33 +519,34 @@ __global__ void __launch_bounds__(128) ll_pair_kernel(LLArgs a) {
     {
 #pragma unroll
         for (int q = 0; q < 9; q++) {
-            const double v = warp_sum((double)gT0[q / 3][q % 3]);
-            if (lane == 0) pl[q] = v;
+            const R v = warp_sum(gT0[q / 3][q % 3]);
+            if (lane == 0) pl[q] = (double)v;
         }
 #pragma unroll
         for (int k = 1; k < 3; k++) {
-            const double v = warp_sum((double)(-twopi * (R)len[0] * cjmul(gD0[k], D0[k]).im));
-            if (lane == 0) pl[9 + k - 1] = v;
+            const R v = warp_sum(-twopi * src.L(0) * cjmul(gD0[k], D0[k]).im);
+            if (lane == 0) pl[9 + k - 1] = (double)v;
         }
     }
-    // per energy: Lambda', Gamma', LL
+    // per energy: Lambda', Gamma' (kernel precision), LL (FP64)
     double* pe = a.part_e + ((size_t)cchunk * a.n_en + e) * kLLPerE;
-    double vals[kLLPerE];
+    R vals[kLLPerE - 1];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        vals[k] = (double)gLa[k];
-        vals[3 + 2 * k] = (double)gLb[k].re;
-        vals[4 + 2 * k] = (double)gLb[k].im;
-        vals[9 + k] = (double)gGa[k];
-        vals[12 + 2 * k] = (double)gGb[k].re;
-        vals[13 + 2 * k] = (double)gGb[k].im;
+        vals[k] = gLa[k];
+        vals[3 + 2 * k] = gLb[k].re;
+        vals[4 + 2 * k] = gLb[k].im;
+        vals[9 + k] = gGa[k];
+        vals[12 + 2 * k] = gGb[k].re;
+        vals[13 + 2 * k] = gGb[k].im;
     }
-    vals[18] = ll;
 #pragma unroll
-    for (int q = 0; q < kLLPerE; q++) {
-        const double v = warp_sum(vals[q]);
-        if (lane == 0) pe[q] = v;
+    for (int q = 0; q < kLLPerE - 1; q++) {
+        const R v = warp_sum(vals[q]);
+        if (lane == 0) pe[q] = (double)v;
     }
+    const double llw = warp_sum(ll);
+    if (lane == 0) pe[kLLPerE - 1] = llw;
 }
 
 // ---------------------------------------------------------- reduction ----
@@ -519,7 +581,12 @@ __global__ void __launch_bounds__(96) ll_layer_kernel(LLArgs a) {
             gK0 += pl[9];
             gK1 += pl[10];
         }
-        layer_eigen(o, E, a.rhoye[l], m, V);
+        // eigen-pairs of this (energy, layer) as solved by the prep kernel
+        const double* ev = a.eig + ((size_t)e * nl + l) * kLLEigWords;
+#pragma unroll
+        for (int q = 0; q < 9; q++) V[q] = ev[q];
+#pragma unroll
+        for (int k = 0; k < 3; k++) m[k] = ev[9 + k];
 #pragma unroll
         for (int q = 0; q < 9; q++) {
             sV[l][q] = V[q];
@@ -732,6 +799,9 @@ struct cp3_loglik {
     double *d_en = nullptr, *d_cos = nullptr, *d_radii = nullptr, *d_fe = nullptr, *d_fm = nullptr, *d_counts = nullptr;
     double *d_tab = nullptr, *d_pe = nullptr, *d_len = nullptr, *d_pl = nullptr, *d_pee = nullptr, *d_out = nullptr;
     double* d_pg = nullptr;
+    double* d_eig = nullptr;
+    float *d_tabf = nullptr, *d_pef = nullptr;
+    float2* d_lenf = nullptr;
     double *d_rhoye = nullptr, *d_yel = nullptr;
     int *d_maxl = nullptr, *d_row = nullptr;
     cp3::OscParams* d_osc = nullptr;
@@ -751,11 +821,15 @@ void ll_free(cp3_loglik* L) {
     L->exec = nullptr;
     L->graph = nullptr;
     void* ptrs[] = {L->d_en, L->d_cos, L->d_radii, L->d_fe, L->d_fm, L->d_counts, L->d_tab, L->d_pe, L->d_len,
-                    L->d_pl, L->d_pee, L->d_out, L->d_pg, L->d_rhoye, L->d_yel, L->d_maxl, L->d_row, L->d_osc};
+                    L->d_pl, L->d_pee, L->d_out, L->d_pg, L->d_rhoye, L->d_yel, L->d_maxl, L->d_row, L->d_osc,
+                    L->d_eig, L->d_tabf, L->d_pef, L->d_lenf};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     L->d_en = L->d_cos = L->d_radii = L->d_fe = L->d_fm = L->d_counts = nullptr;
     L->d_tab = L->d_pe = L->d_len = L->d_pl = L->d_pee = L->d_out = L->d_pg = L->d_rhoye = L->d_yel = nullptr;
+    L->d_eig = nullptr;
+    L->d_tabf = L->d_pef = nullptr;
+    L->d_lenf = nullptr;
     L->d_maxl = L->d_row = nullptr;
     L->d_osc = nullptr;
 }
@@ -795,6 +869,10 @@ cp3::LLArgs ll_args(cp3_loglik* L, int type) {
     a.part_l = L->d_pl;
     a.part_e = L->d_pee;
     a.part_g = L->d_pg;
+    a.eig = L->d_eig;
+    a.tabf = L->mixed ? L->d_tabf : nullptr;
+    a.pef = L->mixed ? L->d_pef : nullptr;
+    a.lenf = L->mixed ? L->d_lenf : nullptr;
     a.out = L->d_out;
     a.layer_row = L->d_row;
     a.n_rows = L->n_rows;
@@ -833,7 +911,12 @@ int ll_setup(cp3_loglik* L, int type) {
         (e = cudaMalloc(&L->d_pl, pl * 8)) || (e = cudaMalloc(&L->d_pee, pee * 8)) ||
         (e = cudaMalloc(&L->d_out, (cp3::kLLMaxParams + 1) * 8)) ||
         (e = cudaMalloc(&L->d_pg, (size_t)L->n_en * (cp3::kLLMaxParams + 1) * 8)) || (e = cudaMalloc(&L->d_rhoye, (cp3::kMaxRows + 1) * 8)) ||
-        (e = cudaMalloc((void**)&L->d_osc, sizeof(cp3::OscParams))))
+        (e = cudaMalloc((void**)&L->d_osc, sizeof(cp3::OscParams))) ||
+        (e = cudaMalloc(&L->d_eig, (size_t)L->n_en_pad * L->nl * cp3::kLLEigWords * 8)))
+        return lcuda(e, "cudaMalloc(loglik)");
+    if (L->mixed &&
+        ((e = cudaMalloc(&L->d_tabf, (size_t)L->n_en_pad * L->nl * cp3::kLLFWords * 4)) ||
+         (e = cudaMalloc(&L->d_pef, (size_t)18 * L->n_en_pad * 4)) || (e = cudaMalloc(&L->d_lenf, len * 8))))
         return lcuda(e, "cudaMalloc(loglik)");
     // capture
     cudaStream_t cs;
@@ -844,7 +927,11 @@ int ll_setup(cp3_loglik* L, int type) {
     if (!e)
         e = cudaMemcpyAsync(L->d_rhoye, L->h_up + sizeof(cp3::OscParams), sizeof(double) * L->nl, cudaMemcpyHostToDevice, cs);
     if (!e) {
-        const int eb = std::max(1, 256 / L->nl);
+        // energies per prep block: enough blocks to spread the FP64
+        // eigen-solves over the GPU (about two per SM), at most 256 threads
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, L->device);
+        const int eb = std::max(1, std::min(256 / L->nl, L->n_en_pad / std::max(1, 2 * sms)));
         const int nbE = (L->n_en_pad + eb - 1) / eb;
         const int nbC = (L->n_cos + L->nl * eb - 1) / (L->nl * eb);
         cp3::ll_prep_kernel<<<nbE + nbC, dim3(L->nl, eb), (size_t)eb * L->nl * 9 * 8, cs>>>(a);

@@ -29,15 +29,18 @@ struct GridTables {
 
 // Thread (l, e) of the energy part: eigen-solve of layer l at energy E, writes
 // kappa (and Lambda'/Gamma' for l = 0, 1), leaves the eigenvectors in `vme`
-// (shared memory) for the overlap pass.
+// (shared memory) for the overlap pass and, if `m_out` is given, the
+// eigenvalues there.
 template <bool MIXED>
 __device__ __forceinline__ void prep_energy_layer(const OscParams& osc, double E, double rhoye, int l, int e,
-                                                  const GridTables& g, double* vme) {
+                                                  const GridTables& g, double* vme, double* m_out = nullptr) {
     const int te = g.te, tile = e / te, lane = e % te;
     const int W = MIXED ? kMixedWords : kFp64Words;
     double m[3], V[9];
     layer_eigen(osc, E, rhoye, m, V);
     for (int w = 0; w < 9; w++) vme[w] = V[w];
+    if (m_out)
+        for (int k = 0; k < 3; k++) m_out[k] = m[k];
     const double k1 = phase_turns_per_km(m[1], m[0], E);
     const double k2 = phase_turns_per_km(m[2], m[0], E);
     const size_t base = ((size_t)tile * g.nl + l) * W * te + lane;
