@@ -50,6 +50,12 @@ SIGNATURES = [
     ("cp3_copy_results_to_host", _I, [_P, _P, _SZ]),
     ("cp3_set_result_buffer", _I, [_P, _P, _SZ]),
     ("cp3_set_host_result_buffer", _I, [_P, _P, _SZ]),
+    ("cp3_set_rate_flux", _I, [_P, _P, _I, _I]),
+    ("cp3_set_rate_bins", _I, [_P, _IP, _IP, _I, _I]),
+    ("cp3_calculate_rates", _I, [_P, _I]),
+    ("cp3_calculate_rates_async", _I, [_P, _I]),
+    ("cp3_rates_device_ptr", _I, [_P, ctypes.POINTER(_P)]),
+    ("cp3_get_rates", _I, [_P, _DP, _SZ]),
     ("cp3_set_stream", _I, [_P, _P]),
     ("cp3_last_launch_count", _I, [_P, _IP]),
     ("cp3_get_maxlayers", _I, [_P, _IP, _I]),

@@ -92,6 +92,16 @@ struct cp3_propagator {
     void* ext_result = nullptr;
     size_t ext_bytes = 0;
     void* ext_host = nullptr;  // caller page-locked host buffer behind ext_result (zero-copy)
+
+    // fused event rates
+    DevBuf<float> d_flux;
+    const float* ext_flux = nullptr;  // caller device flux (instead of d_flux)
+    int flux_mask = 0;
+    bool has_flux = false, has_bins = false;
+    DevBuf<int> d_cbin, d_ebin;
+    DevBuf<double> d_hist;
+    int n_cb = 0, n_eb = 0;
+    const float* rate_flux() const { return ext_flux ? ext_flux : d_flux.p; }
     bool maxl_dirty = true, energy_dirty = true, cosine_dirty = true, density_dirty = true;
 
     // pinned host copy for getProbability (cudapropagator.cuh:73, 168-181)
@@ -225,6 +235,10 @@ int cp3_destroy(cp3_propagator* p) {
     p->d_len.release();
     p->d_result.release();
     p->d_ptab.release();
+    p->d_flux.release();
+    p->d_cbin.release();
+    p->d_ebin.release();
+    p->d_hist.release();
     if (p->h_result) cudaFreeHost(p->h_result);
     for (auto& e : p->ev)
         if (e) cudaEventDestroy(e);
@@ -392,7 +406,11 @@ int cp3_set_host_result_buffer(cp3_propagator* p, void* host, size_t bytes) {
     return CP3_OK;
 }
 
-int cp3_calculate_probabilities_async(cp3_propagator* p, int type) {
+namespace {
+
+// prep + propagate of one calculation on the handle's stream: the nine
+// planes (rates = false) or the fused rate histograms (rates = true).
+int calc_async(cp3_propagator* p, int type, bool rates) {
     if (int rc = check(p)) return rc;
     if (!p->is_set_height)
         return fail(CP3_ERR_STATE, "CudaPropagatorSingle::calculateProbabilities. production height was not set");
@@ -404,7 +422,7 @@ int cp3_calculate_probabilities_async(cp3_propagator* p, int type) {
         return fail(CP3_ERR_STATE, "CudaPropagatorSingle::calculateProbabilities. energy list was not set");
     if (type != CP3_NEUTRINO && type != CP3_ANTINEUTRINO)
         return fail(CP3_ERR_ARGUMENT, "calculateProbabilities: unknown neutrino type");
-    p->results_on_host = false;
+    if (!rates) p->results_on_host = false;
     p->last_launches = 0;
     if (p->n_cos == 0 || p->n_en == 0) return CP3_OK;
     DeviceGuard g(p->device);
@@ -528,18 +546,119 @@ int cp3_calculate_probabilities_async(cp3_propagator* p, int type) {
     ka.nl = nl;
     ka.nl_pad = nl_pad;
     ka.cchunk = cchunk;
-    ka.c23 = pa.osc.c23;
-    ka.s23 = pa.osc.s23;
-    ka.cd = pa.osc.cd;
-    ka.sd = pa.osc.sd;
-    ka.q_c23 = (int)std::llround(ka.c23 * 1073741824.0);
-    ka.q_s23 = (int)std::llround(ka.s23 * 1073741824.0);
-    ka.q_cd = (int)std::llround(ka.cd * 1073741824.0);
-    ka.q_sd = (int)std::llround(ka.sd * 1073741824.0);
-    if ((e = cp3::launch_propagate(p->mixed, ka, te, groups, smem, p->stream)) != cudaSuccess)
+    if (rates) {
+        ka.flux = p->rate_flux();
+        ka.flux_mask = p->flux_mask;
+        ka.cbin = p->d_cbin.p;
+        ka.ebin = p->d_ebin.p;
+        ka.hist = p->d_hist.p;
+        ka.n_cb = p->n_cb;
+        ka.n_eb = p->n_eb;
+        const size_t hb = (size_t)3 * p->n_cb * p->n_eb * sizeof(double);
+        if ((e = cudaMemsetAsync(p->d_hist.p, 0, hb, p->stream)) != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+    }
+    if ((e = cp3::launch_propagate(p->mixed, ka, te, groups, smem, p->stream, rates)) != cudaSuccess)
         return cuda_fail(e, "propagate kernel");
     if (p->timing && (e = cudaEventRecord(p->ev[2], p->stream)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
     p->last_launches = 2;
+    return CP3_OK;
+}
+
+}  // namespace
+
+int cp3_calculate_probabilities_async(cp3_propagator* p, int type) { return calc_async(p, type, false); }
+
+// ------------------------------------------------------------ event rates --
+int cp3_set_rate_flux(cp3_propagator* p, const float* flux, int flavour_mask, int on_device) {
+    if (int rc = check(p)) return rc;
+    if (flavour_mask < 0 || flavour_mask > 7) return fail(CP3_ERR_ARGUMENT, "set_rate_flux: flavour mask must be in 0..7");
+    if (flavour_mask && !flux) return fail(CP3_ERR_ARGUMENT, "set_rate_flux: null flux");
+    DeviceGuard g(p->device);
+    if (g.err != cudaSuccess) return cuda_fail(g.err, "cudaSetDevice");
+    p->ext_flux = nullptr;
+    p->flux_mask = flavour_mask;
+    const size_t plane = (size_t)p->n_cos * p->n_en;
+    if (on_device) {
+        p->ext_flux = flux;
+    } else if (flavour_mask && plane) {
+        cudaError_t e = p->d_flux.ensure(3 * plane);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+        for (int a = 0; a < 3; a++)
+            if (flavour_mask & (1 << a)) {
+                e = cudaMemcpyAsync(p->d_flux.p + a * plane, flux + a * plane, plane * sizeof(float),
+                                    cudaMemcpyHostToDevice, p->stream);
+                if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(flux)");
+            }
+        if ((e = cudaStreamSynchronize(p->stream)) != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+    }
+    p->has_flux = true;
+    return CP3_OK;
+}
+
+int cp3_set_rate_bins(cp3_propagator* p, const int* cos_bin, const int* en_bin, int n_cos_bins, int n_en_bins) {
+    if (int rc = check(p)) return rc;
+    if (n_cos_bins <= 0 || n_en_bins <= 0) return fail(CP3_ERR_ARGUMENT, "set_rate_bins: bin counts must be positive");
+    if ((p->n_cos && !cos_bin) || (p->n_en && !en_bin)) return fail(CP3_ERR_ARGUMENT, "set_rate_bins: null bin list");
+    for (int i = 0; i < p->n_cos; i++)
+        if (cos_bin[i] < -1 || cos_bin[i] >= n_cos_bins)
+            return fail(CP3_ERR_ARGUMENT, "set_rate_bins: cosine bin index out of range (-1 excludes)");
+    for (int i = 0; i < p->n_en; i++)
+        if (en_bin[i] < -1 || en_bin[i] >= n_en_bins)
+            return fail(CP3_ERR_ARGUMENT, "set_rate_bins: energy bin index out of range (-1 excludes)");
+    DeviceGuard g(p->device);
+    if (g.err != cudaSuccess) return cuda_fail(g.err, "cudaSetDevice");
+    cudaError_t e;
+    if ((e = p->d_cbin.ensure(p->n_cos)) != cudaSuccess || (e = p->d_ebin.ensure(p->n_en)) != cudaSuccess ||
+        (e = p->d_hist.ensure((size_t)3 * n_cos_bins * n_en_bins)) != cudaSuccess)
+        return cuda_fail(e, "cudaMalloc");
+    if ((p->n_cos && (e = cudaMemcpyAsync(p->d_cbin.p, cos_bin, sizeof(int) * p->n_cos, cudaMemcpyHostToDevice,
+                                          p->stream)) != cudaSuccess) ||
+        (p->n_en && (e = cudaMemcpyAsync(p->d_ebin.p, en_bin, sizeof(int) * p->n_en, cudaMemcpyHostToDevice,
+                                         p->stream)) != cudaSuccess) ||
+        (e = cudaMemsetAsync(p->d_hist.p, 0, sizeof(double) * 3 * n_cos_bins * n_en_bins, p->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(p->stream)) != cudaSuccess)
+        return cuda_fail(e, "set_rate_bins upload");
+    p->n_cb = n_cos_bins;
+    p->n_eb = n_en_bins;
+    p->has_bins = true;
+    return CP3_OK;
+}
+
+int cp3_calculate_rates_async(cp3_propagator* p, int type) {
+    if (int rc = check(p)) return rc;
+    if (!p->has_flux) return fail(CP3_ERR_STATE, "calculateRates: flux was not set");
+    if (!p->has_bins) return fail(CP3_ERR_STATE, "calculateRates: bins were not set");
+    if (p->n_cos == 0 || p->n_en == 0) {
+        DeviceGuard g(p->device);
+        cudaError_t e = cudaMemsetAsync(p->d_hist.p, 0, sizeof(double) * 3 * p->n_cb * p->n_eb, p->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+    }
+    return calc_async(p, type, true);
+}
+
+int cp3_calculate_rates(cp3_propagator* p, int type) {
+    int rc = cp3_calculate_rates_async(p, type);
+    if (rc != CP3_OK) return rc;
+    return cp3_wait_for_completion(p);
+}
+
+int cp3_rates_device_ptr(cp3_propagator* p, double** dptr) {
+    if (int rc = check(p)) return rc;
+    if (!dptr) return fail(CP3_ERR_ARGUMENT, "null output pointer");
+    if (!p->has_bins) return fail(CP3_ERR_STATE, "rates_device_ptr: bins were not set");
+    *dptr = p->d_hist.p;
+    return CP3_OK;
+}
+
+int cp3_get_rates(cp3_propagator* p, double* host, size_t count) {
+    if (int rc = check(p)) return rc;
+    if (!p->has_bins) return fail(CP3_ERR_STATE, "get_rates: bins were not set");
+    const size_t n = (size_t)3 * p->n_cb * p->n_eb;
+    if (!host || count < n) return fail(CP3_ERR_ARGUMENT, "get_rates: destination smaller than 3*n_cos_bins*n_en_bins");
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaMemcpyAsync(host, p->d_hist.p, n * sizeof(double), cudaMemcpyDeviceToHost, p->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(rates)");
     return CP3_OK;
 }
 

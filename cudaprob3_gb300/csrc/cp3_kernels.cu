@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a) {
 }
 
 // ------------------------------------------------------------ propagate ----
-template <bool MIXED, int TE>
+template <bool MIXED, int TE, bool RATES>
 __global__ void __launch_bounds__(MIXED ? 256 : 128, 3) propagate_kernel(PropArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const TileSmem L = tile_smem(MIXED, TE, a.nl, a.nl_pad, a.cchunk);
@@ -74,7 +74,14 @@ __global__ void __launch_bounds__(MIXED ? 256 : 128, 3) propagate_kernel(PropArg
     j.etile = blockIdx.x;
     j.c0 = blockIdx.y * a.cchunk;
     j.ncl = min(j.c0 + a.cchunk, a.n_cos) - j.c0;
-    process_tile<MIXED, TE>(j, a.nl, a.nl_pad, smem, L);
+    j.flux = a.flux;
+    j.flux_mask = a.flux_mask;
+    j.cbin = a.cbin;
+    j.ebin = a.ebin;
+    j.hist = a.hist;
+    j.n_cb = a.n_cb;
+    j.n_eb = a.n_eb;
+    process_tile<MIXED, TE, RATES>(j, a.nl, a.nl_pad, smem, L);
 }
 
 // ------------------------------------------------------------- launchers ----
@@ -109,33 +116,40 @@ cudaError_t launch_prep(bool mixed, PrepArgs a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-template <bool MIXED, int TE>
+template <bool MIXED, int TE, bool RATES>
 static cudaError_t launch_prop_t(const PropArgs& a, int groups, size_t smem, cudaStream_t s) {
     static bool configured = false;  // one attribute call per instantiation (per process)
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(propagate_kernel<MIXED, TE>,
+        cudaError_t e = cudaFuncSetAttribute(propagate_kernel<MIXED, TE, RATES>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem());
         if (e != cudaSuccess) return e;
         configured = true;
     }
     dim3 grid(a.n_en_pad / TE, (a.n_cos + a.cchunk - 1) / a.cchunk);
     dim3 block(TE, groups);
-    propagate_kernel<MIXED, TE><<<grid, block, smem, s>>>(a);
+    propagate_kernel<MIXED, TE, RATES><<<grid, block, smem, s>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t launch_propagate(bool mixed, const PropArgs& a, int te, int groups, size_t smem, cudaStream_t s) {
-    if (a.n_cos == 0 || a.n_en == 0) return cudaSuccess;
+template <bool RATES>
+static cudaError_t launch_prop_r(bool mixed, const PropArgs& a, int te, int groups, size_t smem, cudaStream_t s) {
     if (mixed) {
-        if (te == 32) return launch_prop_t<true, 32>(a, groups, smem, s);
-        if (te == 64) return launch_prop_t<true, 64>(a, groups, smem, s);
-        if (te == 128) return launch_prop_t<true, 128>(a, groups, smem, s);
+        if (te == 32) return launch_prop_t<true, 32, RATES>(a, groups, smem, s);
+        if (te == 64) return launch_prop_t<true, 64, RATES>(a, groups, smem, s);
+        if (te == 128) return launch_prop_t<true, 128, RATES>(a, groups, smem, s);
     } else {
-        if (te == 32) return launch_prop_t<false, 32>(a, groups, smem, s);
-        if (te == 64) return launch_prop_t<false, 64>(a, groups, smem, s);
-        if (te == 128) return launch_prop_t<false, 128>(a, groups, smem, s);
+        if (te == 32) return launch_prop_t<false, 32, RATES>(a, groups, smem, s);
+        if (te == 64) return launch_prop_t<false, 64, RATES>(a, groups, smem, s);
+        if (te == 128) return launch_prop_t<false, 128, RATES>(a, groups, smem, s);
     }
     return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_propagate(bool mixed, const PropArgs& a, int te, int groups, size_t smem, cudaStream_t s,
+                             bool rates) {
+    if (a.n_cos == 0 || a.n_en == 0) return cudaSuccess;
+    return rates ? launch_prop_r<true>(mixed, a, te, groups, smem, s)
+                 : launch_prop_r<false>(mixed, a, te, groups, smem, s);
 }
 
 }  // namespace cp3

@@ -27,8 +27,13 @@ struct PropArgs {
     const int4* ptab;  // mixed: 257 (Q1.30 cos, Q1.30 sin, float cos, float sin) of 2*pi*j/256
     void* out;
     int n_cos, n_en, n_en_pad, nl, nl_pad, cchunk;
-    double c23, s23, cd, sd;     // FP64 flavour rotation
-    int q_c23, q_s23, q_cd, q_sd;  // the same in Q1.30
+    // fused rates (launch_propagate with rates = true): see TileJob
+    const float* flux;
+    int flux_mask;
+    const int* cbin;
+    const int* ebin;
+    double* hist;
+    int n_cb, n_eb;
 };
 
 size_t propagate_smem_bytes(bool mixed, int te, int nl, int nl_pad, int cchunk);
@@ -40,7 +45,7 @@ int max_dynamic_smem();
 inline int propagate_max_threads(bool mixed) { return mixed ? 256 : 128; }
 cudaError_t launch_prep(bool mixed, PrepArgs a, cudaStream_t s);
 cudaError_t launch_propagate(bool mixed, const PropArgs& a, int te, int groups, size_t smem,
-                             cudaStream_t s);
+                             cudaStream_t s, bool rates = false);
 
 // Message returned by cp3_last_error() on this thread.
 void set_last_error(const std::string& msg);

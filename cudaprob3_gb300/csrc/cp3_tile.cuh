@@ -200,7 +200,7 @@ __device__ __forceinline__ void block_copy16(void* dst, const void* src, int n16
 
 // Shared-memory layout of one tile (bytes); `cchunk` bounds the cosine chunk.
 struct TileSmem {
-    size_t tab, pe, ptab, len, maxl, total;
+    size_t tab, pe, ptab, len, maxl, cbin, total;
 };
 __host__ __device__ inline TileSmem tile_smem(bool mixed, int te, int nl, int nl_pad, int cchunk) {
     const size_t word = mixed ? 4 : 8;
@@ -211,7 +211,8 @@ __host__ __device__ inline TileSmem tile_smem(bool mixed, int te, int nl, int nl
     t.ptab = t.pe + (size_t)kPerEWords * te * word;
     t.len = t.ptab + (mixed ? kPhaseTabBytes : 0);
     t.maxl = t.len + (size_t)cchunk * nl_pad * 8;
-    t.total = (t.maxl + (size_t)cchunk * 4 + 15) / 16 * 16;
+    t.cbin = t.maxl + (size_t)cchunk * 4;
+    t.total = (t.cbin + (size_t)cchunk * 4 + 15) / 16 * 16;
     return t;
 }
 
@@ -228,7 +229,68 @@ struct TileJob {
     void* out;         // grid's [9][n_cos][n_en]
     int n_cos, n_en, n_en_pad;
     int etile, c0, ncl;
+    // fused event rates (process_tile<..., RATES = true>): instead of the
+    // planes, rate_b(c, E) = sum_a flux[a][c][E] P(a -> b) is summed into
+    // hist[b][cbin[c]][ebin[E]] (bin -1: not histogrammed)
+    const float* flux;  // [3][n_cos][n_en], planes whose bit is clear in flux_mask are not read
+    int flux_mask;
+    const int* cbin;    // [n_cos]
+    const int* ebin;    // [n_en]
+    double* hist;       // [3][n_cb][n_eb]
+    int n_cb, n_eb;
 };
+
+// Adds one run of rates (the lanes' sums since the warp's cosine bin `cb`
+// changed) to the histogram.  `cb` is warp-uniform (a warp's lanes share the
+// cosine); `eb` is the lane's energy bin.  When the lanes of equal energy bin
+// form contiguous groups (monotone binning), each group is summed by a
+// segmented butterfly and its first lane adds it: one atomic per bin and
+// flavour; otherwise every lane adds its own sums.  Called by whole warps.
+template <class Acc>
+__device__ __forceinline__ void flush_rates(Acc& s0, Acc& s1, Acc& s2, int cb, int eb, const TileJob& j) {
+    const unsigned full = 0xffffffffu;
+    if (cb >= 0) {
+        const int lane = threadIdx.x & 31;
+        const unsigned grp = __match_any_sync(full, eb);
+        const int lo = __ffs(grp) - 1, hi = 31 - __clz(grp);
+        const unsigned span = (hi - lo == 31) ? full : (((1u << (hi - lo + 1)) - 1u) << lo);
+        if (__all_sync(full, grp == span)) {
+            const int end = hi + 1;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const Acc o0 = __shfl_down_sync(full, s0, off);
+                const Acc o1 = __shfl_down_sync(full, s1, off);
+                const Acc o2 = __shfl_down_sync(full, s2, off);
+                if (lane + off < end) {
+                    s0 += o0;
+                    s1 += o1;
+                    s2 += o2;
+                }
+            }
+            if (lane != lo) eb = -1;
+        }
+        if (eb >= 0) {
+            const size_t pl = (size_t)j.n_cb * j.n_eb;
+            double* h = j.hist + (size_t)cb * j.n_eb + eb;
+            atomicAdd(h, (double)s0);
+            atomicAdd(h + pl, (double)s1);
+            atomicAdd(h + 2 * pl, (double)s2);
+        }
+    }
+    s0 = s1 = s2 = Acc(0);
+}
+
+// Rate of final flavour b at (ci, e) from the nine probabilities.
+template <class Acc, class P>
+__device__ __forceinline__ void add_rates(const TileJob& j, int ci, int e, const P* pr, Acc& s0, Acc& s1, Acc& s2) {
+    const size_t plane = (size_t)j.n_cos * j.n_en, at = (size_t)ci * j.n_en + e;
+    const Acc f0 = (j.flux_mask & 1) ? (Acc)__ldcs(j.flux + at) : Acc(0);
+    const Acc f1 = (j.flux_mask & 2) ? (Acc)__ldcs(j.flux + plane + at) : Acc(0);
+    const Acc f2 = (j.flux_mask & 4) ? (Acc)__ldcs(j.flux + 2 * plane + at) : Acc(0);
+    s0 += f0 * (Acc)pr[0] + f1 * (Acc)pr[3] + f2 * (Acc)pr[6];
+    s1 += f0 * (Acc)pr[1] + f1 * (Acc)pr[4] + f2 * (Acc)pr[7];
+    s2 += f0 * (Acc)pr[2] + f1 * (Acc)pr[5] + f2 * (Acc)pr[8];
+}
 
 template <bool MIXED>
 __device__ __forceinline__ void stage_phase_table(unsigned char* smem, const TileSmem& L, const int4* ptab) {
@@ -238,7 +300,7 @@ __device__ __forceinline__ void stage_phase_table(unsigned char* smem, const Til
     for (int i = t; i < kPhaseTabN + 1; i += nt) s[i] = ptab[i];
 }
 
-template <bool MIXED, int TE>
+template <bool MIXED, int TE, bool RATES = false>
 __device__ __forceinline__ void process_tile(const TileJob& j, int nl, int nl_pad, unsigned char* smem,
                                              const TileSmem& L) {
     using Word = typename std::conditional<MIXED, int, double>::type;
@@ -260,6 +322,10 @@ __device__ __forceinline__ void process_tile(const TileJob& j, int nl, int nl_pa
         const int nlen16 = j.ncl * nl_pad / 2;  // 8-byte entries, nl_pad even
         block_copy16(s_len_raw, (const unsigned char*)j.len + (size_t)j.c0 * nl_pad * 8, nlen16);
         for (int i = t; i < j.ncl; i += nt) s_maxl[i] = j.maxl[j.c0 + i];
+        if (RATES) {
+            int* s_cbin = (int*)(smem + L.cbin);
+            for (int i = t; i < j.ncl; i += nt) s_cbin[i] = j.cbin[j.c0 + i];
+        }
     }
     __syncthreads();
 
@@ -267,6 +333,12 @@ __device__ __forceinline__ void process_tile(const TileJob& j, int nl, int nl_pa
     const int e = j.etile * TE + lane;
     const bool store = e < j.n_en;
     const size_t plane = (size_t)j.n_cos * j.n_en;
+    // fused rates: per-lane sums of the current cosine-bin run (FP32 for the
+    // mixed kernel: a run is a few cosines; FP64 for the FP64 kernel)
+    using Acc = typename std::conditional<MIXED, float, double>::type;
+    Acc r0 = 0, r1 = 0, r2 = 0;
+    int run_cb = -1;
+    const int my_eb = (RATES && store) ? j.ebin[e] : -1;
     for (int cl = threadIdx.y; cl < j.ncl; cl += blockDim.y) {
         const int M = s_maxl[cl];
         const int ci = j.c0 + cl;
@@ -278,7 +350,14 @@ __device__ __forceinline__ void process_tile(const TileJob& j, int nl, int nl_pa
             flavour_block<Q30>(ar, src, M, B);
             float pr[9];
             Q30::complete(B, pr);
-            if (store) {
+            if (RATES) {
+                const int cb = ((const int*)(smem + L.cbin))[cl];
+                if (cb != run_cb) {
+                    flush_rates(r0, r1, r2, run_cb, my_eb, j);
+                    run_cb = cb;
+                }
+                if (cb >= 0 && my_eb >= 0) add_rates(j, ci, e, pr, r0, r1, r2);
+            } else if (store) {
                 float* out = (float*)j.out + (size_t)ci * j.n_en + e;
 #pragma unroll
                 for (int t = 0; t < 9; t++) __stcs(out + (size_t)t * plane, pr[t]);
@@ -291,13 +370,21 @@ __device__ __forceinline__ void process_tile(const TileJob& j, int nl, int nl_pa
             flavour_block<F64>(ar, src, M, B);
             double pr[9];
             F64::complete(B, pr);
-            if (store) {
+            if (RATES) {
+                const int cb = ((const int*)(smem + L.cbin))[cl];
+                if (cb != run_cb) {
+                    flush_rates(r0, r1, r2, run_cb, my_eb, j);
+                    run_cb = cb;
+                }
+                if (cb >= 0 && my_eb >= 0) add_rates(j, ci, e, pr, r0, r1, r2);
+            } else if (store) {
                 double* out = (double*)j.out + (size_t)ci * j.n_en + e;
 #pragma unroll
                 for (int t = 0; t < 9; t++) __stcs(out + (size_t)t * plane, pr[t]);
             }
         }
     }
+    if (RATES) flush_rates(r0, r1, r2, run_cb, my_eb, j);
 }
 
 }  // namespace cp3

@@ -176,6 +176,52 @@ class CudaPropagatorSingle:
         returns to the device buffer.  Pageable memory raises CP3Error."""
         check(self._lib.cp3_set_host_result_buffer(self._h, ctypes.c_void_p(host_ptr), int(nbytes)))
 
+    # ---- fused event rates (no reference counterpart; include/cudaprob3_gb300.h)
+    def setRateFlux(self, flux, flavour_mask=7):
+        """Per-(cosine, energy) weights of the initial flavours e, mu, tau:
+        array [3][n_cosines][n_energies] (float32; planes whose bit is clear
+        in `flavour_mask` are ignored), copied to the device."""
+        f = np.ascontiguousarray(flux, dtype=np.float32)
+        if f.shape != (3, self.n_cosines, self.n_energies):
+            raise ValueError("flux must have shape (3, n_cosines, n_energies)")
+        self._flux_host = f
+        check(self._lib.cp3_set_rate_flux(self._h, f.ctypes.data_as(ctypes.c_void_p), int(flavour_mask), 0))
+
+    def set_rate_flux_device(self, device_ptr, flavour_mask=7):
+        """Flux already on the device (caller-owned [3][n_cos][n_en] float32)."""
+        check(self._lib.cp3_set_rate_flux(self._h, ctypes.c_void_p(device_ptr), int(flavour_mask), 1))
+
+    def setRateBins(self, cos_bin, en_bin, n_cos_bins, n_en_bins):
+        """Histogram bin of every cosine and energy node (-1 leaves it out)."""
+        cb = np.ascontiguousarray(cos_bin, dtype=np.int32)
+        eb = np.ascontiguousarray(en_bin, dtype=np.int32)
+        if cb.shape != (self.n_cosines,) or eb.shape != (self.n_energies,):
+            raise ValueError("one bin index per cosine and per energy node")
+        check(self._lib.cp3_set_rate_bins(self._h, cb.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                          eb.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                          int(n_cos_bins), int(n_en_bins)))
+        self._rate_shape = (3, int(n_cos_bins), int(n_en_bins))
+
+    def calculateRatesAsync(self, ntype):
+        check(self._lib.cp3_calculate_rates_async(self._h, int(ntype)))
+
+    def calculateRates(self, ntype, out=None):
+        """Propagate and histogram rate_b = sum_a flux_a P(a -> b); returns the
+        FP64 histograms [3][n_cos_bins][n_en_bins] (final flavour first)."""
+        check(self._lib.cp3_calculate_rates(self._h, int(ntype)))
+        return self.rates(out)
+
+    def rates(self, out=None):
+        if out is None:
+            out = np.empty(self._rate_shape, dtype=np.float64)
+        check(self._lib.cp3_get_rates(self._h, _dptr(out), out.size))
+        return out
+
+    def rates_device_ptr(self):
+        p = ctypes.c_void_p()
+        check(self._lib.cp3_rates_device_ptr(self._h, ctypes.byref(p)))
+        return p.value
+
     def set_stream(self, stream_handle):
         check(self._lib.cp3_set_stream(self._h, ctypes.c_void_p(stream_handle)))
 

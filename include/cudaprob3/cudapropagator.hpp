@@ -46,7 +46,8 @@ public:
 
     CudaPropagatorSingle(const CudaPropagatorSingle&) = delete;
     CudaPropagatorSingle& operator=(const CudaPropagatorSingle&) = delete;
-    CudaPropagatorSingle(CudaPropagatorSingle&& o) noexcept : Propagator<FLOAT_T>(o), h(o.h), deviceId(o.deviceId) {
+    CudaPropagatorSingle(CudaPropagatorSingle&& o) noexcept
+        : Propagator<FLOAT_T>(o), h(o.h), deviceId(o.deviceId), rateBins(o.rateBins) {
         o.h = nullptr;
     }
     CudaPropagatorSingle& operator=(CudaPropagatorSingle&& o) noexcept {
@@ -55,6 +56,7 @@ public:
             cp3_destroy(h);
             h = o.h;
             deviceId = o.deviceId;
+            rateBins = o.rateBins;
             o.h = nullptr;
         }
         return *this;
@@ -132,6 +134,28 @@ public:
     void setHostResultBuffer(FLOAT_T* host, size_t elements) {
         detail::check(cp3_set_host_result_buffer(alive(), host, elements * sizeof(FLOAT_T)));
     }
+    /// Fused event rates (no reference counterpart): per-(cosine, energy)
+    /// weights flux[3][n_cosines][n_energies] of the initial flavours (planes
+    /// with a clear bit in flavourMask are not read), copied to the device.
+    void setRateFlux(const std::vector<float>& flux, int flavourMask = 7) {
+        if (flux.size() != (size_t)3 * this->n_cosines * this->n_energies)
+            throw std::runtime_error("setRateFlux: flux must hold 3 * n_cosines * n_energies values");
+        detail::check(cp3_set_rate_flux(alive(), flux.data(), flavourMask, 0));
+    }
+    /// Histogram bin of every cosine / energy node (-1 leaves it out).
+    void setRateBins(const std::vector<int>& cosBin, const std::vector<int>& enBin, int nCosBins, int nEnBins) {
+        if (cosBin.size() != (size_t)this->n_cosines || enBin.size() != (size_t)this->n_energies)
+            throw std::runtime_error("setRateBins: one bin index per cosine and per energy node");
+        detail::check(cp3_set_rate_bins(alive(), cosBin.data(), enBin.data(), nCosBins, nEnBins));
+        rateBins = (size_t)3 * nCosBins * nEnBins;
+    }
+    /// Propagate and histogram rate_b = sum_a flux_a P(a -> b) into
+    /// hist[b][cosBin][enBin] (resized to 3 * nCosBins * nEnBins).
+    void calculateRates(NeutrinoType type, std::vector<double>& hist) {
+        detail::check(cp3_calculate_rates(alive(), type == Antineutrino ? CP3_ANTINEUTRINO : CP3_NEUTRINO));
+        hist.resize(rateBins);
+        detail::check(cp3_get_rates(alive(), hist.data(), hist.size()));
+    }
     cp3_propagator* handle() { return h; }
 
 private:
@@ -141,6 +165,7 @@ private:
     }
     cp3_propagator* h = nullptr;
     int deviceId;
+    size_t rateBins = 0;
 };
 
 /// Multi-device propagator (cudapropagator.cuh:258-458): cosines are dealt

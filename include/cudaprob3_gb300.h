@@ -140,6 +140,39 @@ int cp3_set_result_buffer(cp3_propagator* p, void* dptr, size_t bytes);
  * returns to the handle's own device buffer. */
 int cp3_set_host_result_buffer(cp3_propagator* p, void* host, size_t bytes);
 
+/* ---- Fused event rates (no reference counterpart) -------------------------
+ * The reference's caller reads all nine planes back (getProbability,
+ * cudapropagator.cuh:168-181) to weight events.  These entry points do that
+ * weighting inside the propagation kernel, so the planes never leave the SM:
+ *   rate_b(c, E) = sum_a flux[a][c][E] * P(a -> b)(c, E),   a, b in (e, mu, tau)
+ *   hist[b][cos_bin[c]][en_bin[E]] += rate_b(c, E)
+ * FP64 histograms; within a histogram bin the order of the additions is not
+ * fixed (atomics), so results can differ in the last bits between runs. */
+
+/* Flux (any per-(cosine, energy) weight: flux x cross-section x exposure ...)
+ * [3][n_cosines][n_energies] floats, plane a = initial flavour a.  Only planes
+ * whose bit is set in flavour_mask (1 = e, 2 = mu, 4 = tau) are read; the
+ * others count as zero.  on_device = 0: host memory, copied now; 1: a device
+ * pointer the handle keeps using (caller-owned, must outlive the handle's
+ * calculations). */
+int cp3_set_rate_flux(cp3_propagator* p, const float* flux, int flavour_mask, int on_device);
+
+/* Histogram binning: cos_bin[n_cosines] in [-1, n_cos_bins), en_bin[n_energies]
+ * in [-1, n_en_bins); -1 leaves that cosine / energy out.  Monotone bins (each
+ * bin a contiguous range) are the fast case; any assignment is correct. */
+int cp3_set_rate_bins(cp3_propagator* p, const int* cos_bin, const int* en_bin, int n_cos_bins, int n_en_bins);
+
+/* One propagation into the histograms [3][n_cos_bins][n_en_bins] (zeroed
+ * first); the nine planes are not written.  Same preconditions as
+ * cp3_calculate_probabilities, plus flux and bins. */
+int cp3_calculate_rates(cp3_propagator* p, int type);
+int cp3_calculate_rates_async(cp3_propagator* p, int type);
+
+/* Device pointer of the histograms, and a synchronous copy of them into host
+ * memory (count >= 3 * n_cos_bins * n_en_bins doubles). */
+int cp3_rates_device_ptr(cp3_propagator* p, double** dptr);
+int cp3_get_rates(cp3_propagator* p, double* host, size_t count);
+
 /* Run on a caller-owned cudaStream_t (NULL returns to the handle's own stream). */
 int cp3_set_stream(cp3_propagator* p, void* cuda_stream);
 
