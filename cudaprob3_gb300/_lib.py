@@ -41,6 +41,7 @@ SIGNATURES = [
     ("cp3_set_density", _I, [_P, _DP, _DP, _DP, _I]),
     ("cp3_set_density_from_file", _I, [_P, ctypes.c_char_p]),
     ("cp3_set_production_height", _I, [_P, _D]),
+    ("cp3_set_production_heights", _I, [_P, _DP, _DP, _I]),
     ("cp3_calculate_probabilities", _I, [_P, _I]),
     ("cp3_calculate_probabilities_async", _I, [_P, _I]),
     ("cp3_wait_for_completion", _I, [_P]),

@@ -102,6 +102,13 @@ struct cp3_propagator {
     DevBuf<double> d_hist;
     int n_cb = 0, n_eb = 0;
     const float* rate_flux() const { return ext_flux ? ext_flux : d_flux.p; }
+
+    // production-height distribution (n_h > 1; otherwise the single height_cm)
+    std::vector<double> heights_cm, height_w;
+    int n_h = 0;
+    bool heights_dirty = false;
+    DevBuf<double> d_heights;
+    DevBuf<unsigned char> d_hw, d_lenh;
     bool maxl_dirty = true, energy_dirty = true, cosine_dirty = true, density_dirty = true;
 
     // pinned host copy for getProbability (cudapropagator.cuh:73, 168-181)
@@ -239,6 +246,9 @@ int cp3_destroy(cp3_propagator* p) {
     p->d_cbin.release();
     p->d_ebin.release();
     p->d_hist.release();
+    p->d_heights.release();
+    p->d_hw.release();
+    p->d_lenh.release();
     if (p->h_result) cudaFreeHost(p->h_result);
     for (auto& e : p->ev)
         if (e) cudaEventDestroy(e);
@@ -267,6 +277,36 @@ int cp3_set_production_height(cp3_propagator* p, double height_km) {
     if (!p->is_set_cosine) return fail(CP3_ERR_STATE, "must set cosine list before production height");
     if (!std::isfinite(height_km)) return fail(CP3_ERR_ARGUMENT, "setProductionHeight: height must be finite");
     p->height_cm = height_km * 100000.0;
+    p->is_set_height = true;
+    p->n_h = 0;
+    return CP3_OK;
+}
+
+int cp3_set_production_heights(cp3_propagator* p, const double* heights_km, const double* weights, int n) {
+    if (int rc = check(p)) return rc;
+    if (!p->is_set_cosine) return fail(CP3_ERR_STATE, "must set cosine list before production height");
+    if (n < 1 || n > CP3_MAX_HEIGHTS)
+        return fail(CP3_ERR_ARGUMENT, "setProductionHeights: between 1 and CP3_MAX_HEIGHTS heights");
+    if (!heights_km || !weights) return fail(CP3_ERR_ARGUMENT, "setProductionHeights: null list");
+    double wsum = 0.0;
+    for (int i = 0; i < n; i++) {
+        if (!std::isfinite(heights_km[i]) || heights_km[i] < 0.0)
+            return fail(CP3_ERR_ARGUMENT, "setProductionHeights: heights must be finite and >= 0");
+        if (!std::isfinite(weights[i]) || weights[i] < 0.0)
+            return fail(CP3_ERR_ARGUMENT, "setProductionHeights: weights must be finite and >= 0");
+        wsum += weights[i];
+    }
+    if (!(wsum > 0.0)) return fail(CP3_ERR_ARGUMENT, "setProductionHeights: weights must not all be zero");
+    if (n == 1) return cp3_set_production_height(p, heights_km[0]);
+    p->heights_cm.resize(n);
+    p->height_w.resize(n);
+    for (int i = 0; i < n; i++) {
+        p->heights_cm[i] = heights_km[i] * 100000.0;
+        p->height_w[i] = weights[i] / wsum;
+    }
+    p->height_cm = p->heights_cm[0];
+    p->n_h = n;
+    p->heights_dirty = true;
     p->is_set_height = true;
     return CP3_OK;
 }
@@ -422,6 +462,9 @@ int calc_async(cp3_propagator* p, int type, bool rates) {
         return fail(CP3_ERR_STATE, "CudaPropagatorSingle::calculateProbabilities. energy list was not set");
     if (type != CP3_NEUTRINO && type != CP3_ANTINEUTRINO)
         return fail(CP3_ERR_ARGUMENT, "calculateProbabilities: unknown neutrino type");
+    if (rates && p->n_h > 1)
+        return fail(CP3_ERR_STATE, "calculateRates: not available with a production-height distribution");
+    const int mode = rates ? 1 : (p->n_h > 1 ? 2 : 0);
     if (!rates) p->results_on_host = false;
     p->last_launches = 0;
     if (p->n_cos == 0 || p->n_en == 0) return CP3_OK;
@@ -488,6 +531,29 @@ int calc_async(cp3_propagator* p, int type, bool rates) {
     if ((e = p->d_pe.ensure((size_t)cp3::kPerEWords * n_en_pad * word)) != cudaSuccess)
         return cuda_fail(e, "cudaMalloc");
     if ((e = p->d_len.ensure((size_t)p->n_cos * nl_pad * 8)) != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    if (mode == 2) {
+        const int nh = p->n_h;
+        if ((e = p->d_heights.ensure(nh)) != cudaSuccess || (e = p->d_hw.ensure((size_t)nh * 8)) != cudaSuccess ||
+            (e = p->d_lenh.ensure((size_t)p->n_cos * nh * 8)) != cudaSuccess)
+            return cuda_fail(e, "cudaMalloc");
+        if (p->heights_dirty) {
+            std::vector<unsigned char> wbuf((size_t)nh * 8);
+            for (int i = 0; i < nh; i++) {
+                if (p->mixed)
+                    ((float*)wbuf.data())[i] = (float)p->height_w[i];
+                else
+                    ((double*)wbuf.data())[i] = p->height_w[i];
+            }
+            if ((e = cudaMemcpyAsync(p->d_heights.p, p->heights_cm.data(), sizeof(double) * nh,
+                                     cudaMemcpyHostToDevice, p->stream)) != cudaSuccess ||
+                (e = cudaMemcpyAsync(p->d_hw.p, wbuf.data(), wbuf.size(), cudaMemcpyHostToDevice, p->stream)) !=
+                    cudaSuccess)
+                return cuda_fail(e, "cudaMemcpyAsync(heights)");
+            // the staged copy must finish before `wbuf` leaves scope
+            if ((e = cudaStreamSynchronize(p->stream)) != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+            p->heights_dirty = false;
+        }
+    }
 
     cp3::PrepArgs pa{};
     pa.pb.n_cos = p->n_cos;
@@ -529,6 +595,11 @@ int calc_async(cp3_propagator* p, int type, bool rates) {
     pa.tab = p->d_tab.p;
     pa.pe = p->d_pe.p;
     pa.len = p->d_len.p;
+    if (mode == 2) {
+        pa.heights_cm = p->d_heights.p;
+        pa.n_h = p->n_h;
+        pa.lenh = p->d_lenh.p;
+    }
     if (p->timing && (e = cudaEventRecord(p->ev[0], p->stream)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
     if ((e = cp3::launch_prep(p->mixed, pa, p->stream)) != cudaSuccess) return cuda_fail(e, "prep kernel");
     if (p->timing && (e = cudaEventRecord(p->ev[1], p->stream)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
@@ -557,7 +628,12 @@ int calc_async(cp3_propagator* p, int type, bool rates) {
         const size_t hb = (size_t)3 * p->n_cb * p->n_eb * sizeof(double);
         if ((e = cudaMemsetAsync(p->d_hist.p, 0, hb, p->stream)) != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
     }
-    if ((e = cp3::launch_propagate(p->mixed, ka, te, groups, smem, p->stream, rates)) != cudaSuccess)
+    if (mode == 2) {
+        ka.lenh = p->d_lenh.p;
+        ka.hw = p->d_hw.p;
+        ka.n_h = p->n_h;
+    }
+    if ((e = cp3::launch_propagate(p->mixed, ka, te, groups, smem, p->stream, mode)) != cudaSuccess)
         return cuda_fail(e, "propagate kernel");
     if (p->timing && (e = cudaEventRecord(p->ev[2], p->stream)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
     p->last_launches = 2;

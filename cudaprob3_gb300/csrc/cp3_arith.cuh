@@ -129,6 +129,17 @@ struct Q30 {
         out[3] = to_prob(q01); out[4] = to_prob(q11); out[5] = to_prob(q21);
         out[6] = to_prob(q02); out[7] = to_prob(q12); out[8] = to_prob(q22);
     }
+    // averages over production heights: |z|^2 as a float (one rounding of the
+    // exact Q2.60 value), weighted sums in FP32, completion of the averaged
+    // block (the completion is linear, so averaging commutes with it)
+    using Acc = float;
+    static __device__ __forceinline__ float prob(C z) { return __ll2float_rn(norm2(z)) * 8.673617379884035e-19f; }
+    static __device__ __forceinline__ void complete_avg(float q00, float q01, float q10, float q11, float out[9]) {
+        out[0] = q00; out[1] = q10; out[2] = fmaxf(1.0f - q00 - q10, 0.0f);
+        out[3] = q01; out[4] = q11; out[5] = fmaxf(1.0f - q01 - q11, 0.0f);
+        out[6] = fmaxf(1.0f - q00 - q01, 0.0f); out[7] = fmaxf(1.0f - q10 - q11, 0.0f);
+        out[8] = fmaxf((q00 + q01) + (q10 + q11) - 1.0f, 0.0f);
+    }
 };
 
 // Q1.30 cos/sin of 2*pi*t for a phase t = kappa * L given in turns as two
@@ -251,6 +262,15 @@ struct F64 {
         out[0] = q00; out[1] = q10; out[2] = fmax(q20, 0.0);
         out[3] = q01; out[4] = q11; out[5] = fmax(q21, 0.0);
         out[6] = fmax(q02, 0.0); out[7] = fmax(q12, 0.0); out[8] = fmax(q22, 0.0);
+    }
+    using Acc = double;
+    static __device__ __forceinline__ double prob(C z) { return fma(z.re, z.re, z.im * z.im); }
+    static __device__ __forceinline__ void complete_avg(double q00, double q01, double q10, double q11,
+                                                        double out[9]) {
+        out[0] = q00; out[1] = q10; out[2] = fmax(1.0 - q00 - q10, 0.0);
+        out[3] = q01; out[4] = q11; out[5] = fmax(1.0 - q01 - q11, 0.0);
+        out[6] = fmax(1.0 - q00 - q01, 0.0); out[7] = fmax(1.0 - q10 - q11, 0.0);
+        out[8] = fmax(q00 + q01 + q10 + q11 - 1.0, 0.0);
     }
 };
 

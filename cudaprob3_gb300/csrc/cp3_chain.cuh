@@ -20,49 +20,13 @@
 
 namespace cp3 {
 
-// Src provides, for the current pair:
-//   void phase(int l, R& c1, R& s1, R& n1, R& c2, R& s2, R& n2)  e^{i psi_k}, n = -s
-//   void phase_acc(..., Turns& acc)   the same, adding psi_1 + psi_2 (turns) to acc
-//   void turns_phase(const Turns& acc, R& c, R& s)               e^{2 pi i acc}
-//   R T(int l, int i, int j)     overlap V_{l+1}^T V_l
-//   R La(int j)                  row 0 of W V_1 (real)
-//   C Lb(int j)                  row 1 of W V_1
-//   R Ga(int k)                  column 0 of V_0^T W^dagger (real)
-//   C Gb(int k)                  column 1 of V_0^T W^dagger
-//
-// Only the 2x2 block S_f[out][in], out, in in {e, mu}, is formed: S_f is
-// unitary, so the 3x3 matrix of |S_f|^2 is doubly stochastic and its other
-// five entries follow from this block (complete_probabilities).
+// G = Y^T D_M Y (symmetric, entries 00 01 02 11 12 22) of a pair that
+// crosses M >= 1 shells, Y = T_{M-1} D_{M-1} ... T_1 D_1.
 template <class P, class Src>
-__device__ __forceinline__ void flavour_block(const P& ar, const Src& src, int M, typename P::C B[4]) {
+__device__ __forceinline__ void chain_G(const P& ar, const Src& src, int M, typename P::C G[6]) {
     using R = typename P::R;
     using C = typename P::C;
     R c1, s1, n1, c2, s2, n2;
-    // X' = T_0 D_0 Gamma' (3x2), or D_0 Gamma' when only the atmosphere is crossed
-    src.phase(0, c1, s1, n1, c2, s2, n2);
-    C g0[3], g1[3];  // D_0 Gamma': columns 0 and 1
-    g0[0] = P::creal(src.Ga(0));
-    g0[1] = ar.mulRC(src.Ga(1), C{c1, s1});
-    g0[2] = ar.mulRC(src.Ga(2), C{c2, s2});
-    g1[0] = src.Gb(0);
-    g1[1] = ar.mulPhase(src.Gb(1), c1, s1, n1);
-    g1[2] = ar.mulPhase(src.Gb(2), c2, s2, n2);
-    if (M == 0) {
-        // S_r = V_0 D_0 V_0^T, so the block is Gamma'^dagger (D_0 Gamma')
-        const C a0 = P::creal(src.Ga(0)), a1 = P::creal(src.Ga(1)), a2 = P::creal(src.Ga(2));
-        const C b0 = P::conj(src.Gb(0)), b1 = P::conj(src.Gb(1)), b2 = P::conj(src.Gb(2));
-        B[0] = ar.dotCC(a0, a1, a2, g0[0], g0[1], g0[2]);
-        B[1] = ar.dotCC(a0, a1, a2, g1[0], g1[1], g1[2]);
-        B[2] = ar.dotCC(b0, b1, b2, g0[0], g0[1], g0[2]);
-        B[3] = ar.dotCC(b0, b1, b2, g1[0], g1[1], g1[2]);
-        return;
-    }
-    C x0[3], x1[3];  // T_0 (D_0 Gamma')
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        x0[i] = ar.dotRC(src.T(0, i, 0), src.T(0, i, 1), src.T(0, i, 2), g0[0], g0[1], g0[2]);
-        x1[i] = ar.dotRC(src.T(0, i, 0), src.T(0, i, 1), src.T(0, i, 2), g1[0], g1[1], g1[2]);
-    }
     C Y[9];
     if (M >= 2) {
         // Only columns 0 and 1 of Y are propagated; Y is unitary with
@@ -103,7 +67,6 @@ __device__ __forceinline__ void flavour_block(const P& ar, const Src& src, int M
     }
     // G = Y^T D_M Y (symmetric)
     src.phase(M, c1, s1, n1, c2, s2, n2);
-    C G[6];  // 00 01 02 11 12 22
     {
         C Z[9];
 #pragma unroll
@@ -118,6 +81,54 @@ __device__ __forceinline__ void flavour_block(const P& ar, const Src& src, int M
 #pragma unroll
             for (int j = i; j < 3; j++) G[g++] = ar.dotCC(Y[i], Y[3 + i], Y[6 + i], Z[j], Z[3 + j], Z[6 + j]);
     }
+}
+
+// Src provides, for the current pair:
+//   void phase(int l, R& c1, R& s1, R& n1, R& c2, R& s2, R& n2)  e^{i psi_k}, n = -s
+//   void phase_acc(..., Turns& acc)   the same, adding psi_1 + psi_2 (turns) to acc
+//   void turns_phase(const Turns& acc, R& c, R& s)               e^{2 pi i acc}
+//   void phase_len(int l, Len L, R& c1, ...)   e^{i psi_k} of layer l for a given length
+//   R T(int l, int i, int j)     overlap V_{l+1}^T V_l
+//   R La(int j)                  row 0 of W V_1 (real)
+//   C Lb(int j)                  row 1 of W V_1
+//   R Ga(int k)                  column 0 of V_0^T W^dagger (real)
+//   C Gb(int k)                  column 1 of V_0^T W^dagger
+//
+// Only the 2x2 block S_f[out][in], out, in in {e, mu}, is formed: S_f is
+// unitary, so the 3x3 matrix of |S_f|^2 is doubly stochastic and its other
+// five entries follow from this block (complete_probabilities).
+template <class P, class Src>
+__device__ __forceinline__ void flavour_block(const P& ar, const Src& src, int M, typename P::C B[4]) {
+    using R = typename P::R;
+    using C = typename P::C;
+    R c1, s1, n1, c2, s2, n2;
+    // X' = T_0 D_0 Gamma' (3x2), or D_0 Gamma' when only the atmosphere is crossed
+    src.phase(0, c1, s1, n1, c2, s2, n2);
+    C g0[3], g1[3];  // D_0 Gamma': columns 0 and 1
+    g0[0] = P::creal(src.Ga(0));
+    g0[1] = ar.mulRC(src.Ga(1), C{c1, s1});
+    g0[2] = ar.mulRC(src.Ga(2), C{c2, s2});
+    g1[0] = src.Gb(0);
+    g1[1] = ar.mulPhase(src.Gb(1), c1, s1, n1);
+    g1[2] = ar.mulPhase(src.Gb(2), c2, s2, n2);
+    if (M == 0) {
+        // S_r = V_0 D_0 V_0^T, so the block is Gamma'^dagger (D_0 Gamma')
+        const C a0 = P::creal(src.Ga(0)), a1 = P::creal(src.Ga(1)), a2 = P::creal(src.Ga(2));
+        const C b0 = P::conj(src.Gb(0)), b1 = P::conj(src.Gb(1)), b2 = P::conj(src.Gb(2));
+        B[0] = ar.dotCC(a0, a1, a2, g0[0], g0[1], g0[2]);
+        B[1] = ar.dotCC(a0, a1, a2, g1[0], g1[1], g1[2]);
+        B[2] = ar.dotCC(b0, b1, b2, g0[0], g0[1], g0[2]);
+        B[3] = ar.dotCC(b0, b1, b2, g1[0], g1[1], g1[2]);
+        return;
+    }
+    C x0[3], x1[3];  // T_0 (D_0 Gamma')
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        x0[i] = ar.dotRC(src.T(0, i, 0), src.T(0, i, 1), src.T(0, i, 2), g0[0], g0[1], g0[2]);
+        x1[i] = ar.dotRC(src.T(0, i, 0), src.T(0, i, 1), src.T(0, i, 2), g1[0], g1[1], g1[2]);
+    }
+    C G[6];  // Y^T D_M Y: 00 01 02 11 12 22
+    chain_G(ar, src, M, G);
     // X = G X' (3x2)
     C X0[3], X1[3];
     X0[0] = ar.dotCC(G[0], G[1], G[2], x0[0], x0[1], x0[2]);
@@ -131,6 +142,64 @@ __device__ __forceinline__ void flavour_block(const P& ar, const Src& src, int M
     B[1] = ar.dotRC(src.La(0), src.La(1), src.La(2), X1[0], X1[1], X1[2]);
     B[2] = ar.dotCC(src.Lb(0), src.Lb(1), src.Lb(2), X0[0], X0[1], X0[2]);
     B[3] = ar.dotCC(src.Lb(0), src.Lb(1), src.Lb(2), X1[0], X1[1], X1[2]);
+}
+
+// Probabilities of one pair averaged over production heights h with weights
+// w_h (sum 1).  Only the atmosphere segment depends on h (physics.hpp:613-616),
+// so the block factors as B(h) = R D_0(h) Gamma' with R = Lambda' G T_0 (or
+// Gamma'^dagger when no shell is crossed): the chain runs once, each height
+// costs one phase pair and a 2x3 by 3x2 product.  `lenh` holds the pair's
+// atmosphere length at every height in the Src's length format; the averaged
+// |B|^2 are completed to the nine probabilities (the completion is linear).
+template <class P, class Src, class LenT, class WT>
+__device__ __forceinline__ void flavour_probs_heights(const P& ar, const Src& src, int M, int H, const LenT* lenh,
+                                                      const WT* w, typename P::Acc out[9]) {
+    using R = typename P::R;
+    using C = typename P::C;
+    using A = typename P::Acc;
+    C R0[3], R1[3];
+    if (M == 0) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            R0[k] = P::creal(src.Ga(k));
+            R1[k] = P::conj(src.Gb(k));
+        }
+    } else {
+        C G[6];
+        chain_G(ar, src, M, G);
+        // rows of Lambda' G (G symmetric: column j = row j)
+        C l0[3], l1[3];
+        l0[0] = ar.dotRC(src.La(0), src.La(1), src.La(2), G[0], G[1], G[2]);
+        l0[1] = ar.dotRC(src.La(0), src.La(1), src.La(2), G[1], G[3], G[4]);
+        l0[2] = ar.dotRC(src.La(0), src.La(1), src.La(2), G[2], G[4], G[5]);
+        l1[0] = ar.dotCC(src.Lb(0), src.Lb(1), src.Lb(2), G[0], G[1], G[2]);
+        l1[1] = ar.dotCC(src.Lb(0), src.Lb(1), src.Lb(2), G[1], G[3], G[4]);
+        l1[2] = ar.dotCC(src.Lb(0), src.Lb(1), src.Lb(2), G[2], G[4], G[5]);
+        // times T_0: R[r][k] = sum_j (Lambda' G)[r][j] T_0[j][k]
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            R0[k] = ar.dotRC(src.T(0, 0, k), src.T(0, 1, k), src.T(0, 2, k), l0[0], l0[1], l0[2]);
+            R1[k] = ar.dotRC(src.T(0, 0, k), src.T(0, 1, k), src.T(0, 2, k), l1[0], l1[1], l1[2]);
+        }
+    }
+    A q00 = 0, q01 = 0, q10 = 0, q11 = 0;
+    for (int h = 0; h < H; h++) {
+        R c1, s1, n1, c2, s2, n2;
+        src.phase_len(0, lenh[h], c1, s1, n1, c2, s2, n2);
+        C g0[3], g1[3];  // D_0(h) Gamma'
+        g0[0] = P::creal(src.Ga(0));
+        g0[1] = ar.mulRC(src.Ga(1), C{c1, s1});
+        g0[2] = ar.mulRC(src.Ga(2), C{c2, s2});
+        g1[0] = src.Gb(0);
+        g1[1] = ar.mulPhase(src.Gb(1), c1, s1, n1);
+        g1[2] = ar.mulPhase(src.Gb(2), c2, s2, n2);
+        const A wh = (A)w[h];
+        q00 += wh * P::prob(ar.dotCC(R0[0], R0[1], R0[2], g0[0], g0[1], g0[2]));
+        q01 += wh * P::prob(ar.dotCC(R0[0], R0[1], R0[2], g1[0], g1[1], g1[2]));
+        q10 += wh * P::prob(ar.dotCC(R1[0], R1[1], R1[2], g0[0], g0[1], g0[2]));
+        q11 += wh * P::prob(ar.dotCC(R1[0], R1[1], R1[2], g1[0], g1[1], g1[2]));
+    }
+    P::complete_avg(q00, q01, q10, q11, out);
 }
 
 }  // namespace cp3

@@ -52,12 +52,25 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a) {
         const int c = (blockIdx.x - a.n_energy_blocks) * (blockDim.x * blockDim.y) + threadIdx.y * blockDim.x +
                       threadIdx.x;
         if (c >= a.pb.n_cos) return;
-        prep_cosine<MIXED>(a.pb.cosines[c], a.pb.maxlayers[c], a.pb.radii, a.pb.height_cm, c, g);
+        const double cz = a.pb.cosines[c];
+        const int M = a.pb.maxlayers[c];
+        prep_cosine<MIXED>(cz, M, a.pb.radii, a.pb.height_cm, c, g);
+        // atmosphere segment at every production height (physics.hpp:613-616, 561-562)
+        for (int h = 0; h < a.n_h; h++) {
+            const double L0 = layer_length_km(a.pb.radii, 0, M, cz, path_length_cm(cz, a.heights_cm[h]));
+            const size_t idx = (size_t)c * a.n_h + h;
+            if (MIXED) {
+                const float hi = (float)L0;
+                ((float2*)a.lenh)[idx] = make_float2(hi, (float)(L0 - (double)hi));
+            } else {
+                ((double*)a.lenh)[idx] = L0;
+            }
+        }
     }
 }
 
 // ------------------------------------------------------------ propagate ----
-template <bool MIXED, int TE, bool RATES>
+template <bool MIXED, int TE, int MODE>
 __global__ void __launch_bounds__(MIXED ? 256 : 128, 3) propagate_kernel(PropArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const TileSmem L = tile_smem(MIXED, TE, a.nl, a.nl_pad, a.cchunk);
@@ -81,7 +94,10 @@ __global__ void __launch_bounds__(MIXED ? 256 : 128, 3) propagate_kernel(PropArg
     j.hist = a.hist;
     j.n_cb = a.n_cb;
     j.n_eb = a.n_eb;
-    process_tile<MIXED, TE, RATES>(j, a.nl, a.nl_pad, smem, L);
+    j.lenh = a.lenh;
+    j.hw = a.hw;
+    j.n_h = a.n_h;
+    process_tile<MIXED, TE, MODE>(j, a.nl, a.nl_pad, smem, L);
 }
 
 // ------------------------------------------------------------- launchers ----
@@ -116,40 +132,41 @@ cudaError_t launch_prep(bool mixed, PrepArgs a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-template <bool MIXED, int TE, bool RATES>
+template <bool MIXED, int TE, int MODE>
 static cudaError_t launch_prop_t(const PropArgs& a, int groups, size_t smem, cudaStream_t s) {
     static bool configured = false;  // one attribute call per instantiation (per process)
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(propagate_kernel<MIXED, TE, RATES>,
+        cudaError_t e = cudaFuncSetAttribute(propagate_kernel<MIXED, TE, MODE>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem());
         if (e != cudaSuccess) return e;
         configured = true;
     }
     dim3 grid(a.n_en_pad / TE, (a.n_cos + a.cchunk - 1) / a.cchunk);
     dim3 block(TE, groups);
-    propagate_kernel<MIXED, TE, RATES><<<grid, block, smem, s>>>(a);
+    propagate_kernel<MIXED, TE, MODE><<<grid, block, smem, s>>>(a);
     return cudaGetLastError();
 }
 
-template <bool RATES>
+template <int MODE>
 static cudaError_t launch_prop_r(bool mixed, const PropArgs& a, int te, int groups, size_t smem, cudaStream_t s) {
     if (mixed) {
-        if (te == 32) return launch_prop_t<true, 32, RATES>(a, groups, smem, s);
-        if (te == 64) return launch_prop_t<true, 64, RATES>(a, groups, smem, s);
-        if (te == 128) return launch_prop_t<true, 128, RATES>(a, groups, smem, s);
+        if (te == 32) return launch_prop_t<true, 32, MODE>(a, groups, smem, s);
+        if (te == 64) return launch_prop_t<true, 64, MODE>(a, groups, smem, s);
+        if (te == 128) return launch_prop_t<true, 128, MODE>(a, groups, smem, s);
     } else {
-        if (te == 32) return launch_prop_t<false, 32, RATES>(a, groups, smem, s);
-        if (te == 64) return launch_prop_t<false, 64, RATES>(a, groups, smem, s);
-        if (te == 128) return launch_prop_t<false, 128, RATES>(a, groups, smem, s);
+        if (te == 32) return launch_prop_t<false, 32, MODE>(a, groups, smem, s);
+        if (te == 64) return launch_prop_t<false, 64, MODE>(a, groups, smem, s);
+        if (te == 128) return launch_prop_t<false, 128, MODE>(a, groups, smem, s);
     }
     return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_propagate(bool mixed, const PropArgs& a, int te, int groups, size_t smem, cudaStream_t s,
-                             bool rates) {
+                             int mode) {
     if (a.n_cos == 0 || a.n_en == 0) return cudaSuccess;
-    return rates ? launch_prop_r<true>(mixed, a, te, groups, smem, s)
-                 : launch_prop_r<false>(mixed, a, te, groups, smem, s);
+    if (mode == kModeRates) return launch_prop_r<kModeRates>(mixed, a, te, groups, smem, s);
+    if (mode == kModeHeights) return launch_prop_r<kModeHeights>(mixed, a, te, groups, smem, s);
+    return launch_prop_r<kModePlanes>(mixed, a, te, groups, smem, s);
 }
 
 }  // namespace cp3

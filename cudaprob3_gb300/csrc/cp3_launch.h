@@ -17,6 +17,10 @@ struct PrepArgs {
     void* pe;   // per-energy V_0, V_1
     void* len;  // per-(cosine, layer) lengths
     int n_energy_blocks;  // set by launch_prep
+    // production-height average: atmosphere length of every cosine at each height
+    const double* heights_cm;  // [n_h] or null
+    int n_h;
+    void* lenh;                // [n_cos][n_h] float2 hi/lo (mixed) or double
 };
 
 struct PropArgs {
@@ -34,6 +38,10 @@ struct PropArgs {
     const int* ebin;
     double* hist;
     int n_cb, n_eb;
+    // production-height average (mode kModeHeights): see TileJob
+    const void* lenh;
+    const void* hw;
+    int n_h;
 };
 
 size_t propagate_smem_bytes(bool mixed, int te, int nl, int nl_pad, int cchunk);
@@ -44,8 +52,9 @@ int max_dynamic_smem();
 // Largest block (threads) the propagate kernel of a precision accepts.
 inline int propagate_max_threads(bool mixed) { return mixed ? 256 : 128; }
 cudaError_t launch_prep(bool mixed, PrepArgs a, cudaStream_t s);
+// mode: 0 planes, 1 fused rates, 2 planes averaged over production heights
 cudaError_t launch_propagate(bool mixed, const PropArgs& a, int te, int groups, size_t smem,
-                             cudaStream_t s, bool rates = false);
+                             cudaStream_t s, int mode = 0);
 
 // Message returned by cp3_last_error() on this thread.
 void set_last_error(const std::string& msg);

@@ -126,7 +126,10 @@ struct MixedSrc {
     __device__ __forceinline__ int Ga(int k) const { return pe[(9 + k) * TE]; }
     __device__ __forceinline__ Q30::C Gb(int k) const { return Q30::C{pe[(12 + 2 * k) * TE], pe[(13 + 2 * k) * TE]}; }
     __device__ __forceinline__ void phase(int l, int& c1, int& s1, int& n1, int& c2, int& s2, int& n2) const {
-        const float2 L = len[l];
+        phase_len(l, len[l], c1, s1, n1, c2, s2, n2);
+    }
+    __device__ __forceinline__ void phase_len(int l, float2 L, int& c1, int& s1, int& n1, int& c2, int& s2,
+                                              int& n2) const {
         const int* k = tab + (l * kMixedWords + 9) * TE;
         phase_q30(__int_as_float(k[0]), __int_as_float(k[TE]), L.x, L.y, ptab, c1, s1);
         phase_q30(__int_as_float(k[2 * TE]), __int_as_float(k[3 * TE]), L.x, L.y, ptab, c2, s2);
@@ -165,7 +168,10 @@ struct F64Src {
     __device__ __forceinline__ F64::C Gb(int k) const { return F64::C{pe[(12 + 2 * k) * TE], pe[(13 + 2 * k) * TE]}; }
     __device__ __forceinline__ void phase(int l, double& c1, double& s1, double& n1, double& c2, double& s2,
                                           double& n2) const {
-        const double L = len[l];
+        phase_len(l, len[l], c1, s1, n1, c2, s2, n2);
+    }
+    __device__ __forceinline__ void phase_len(int l, double L, double& c1, double& s1, double& n1, double& c2,
+                                              double& s2, double& n2) const {
         const double* k = tab + (l * kFp64Words + 9) * TE;
         phase_f64(k[0], L, c1, s1);
         phase_f64(k[TE], L, c2, s2);
@@ -238,7 +244,17 @@ struct TileJob {
     const int* ebin;    // [n_en]
     double* hist;       // [3][n_cb][n_eb]
     int n_cb, n_eb;
+    // production-height average (process_tile<..., kModeHeights>): the
+    // atmosphere length of every cosine at each of n_h heights and the weights
+    const void* lenh;   // [n_cos][n_h] float2 hi/lo (mixed) or double
+    const void* hw;     // [n_h] float (mixed) or double, sum 1
+    int n_h;
 };
+
+// What process_tile does with each pair's probabilities.
+constexpr int kModePlanes = 0;   // store the nine planes
+constexpr int kModeRates = 1;    // fused event-rate histograms
+constexpr int kModeHeights = 2;  // planes averaged over production heights
 
 // Adds one run of rates (the lanes' sums since the warp's cosine bin `cb`
 // changed) to the histogram.  `cb` is warp-uniform (a warp's lanes share the
@@ -300,9 +316,10 @@ __device__ __forceinline__ void stage_phase_table(unsigned char* smem, const Til
     for (int i = t; i < kPhaseTabN + 1; i += nt) s[i] = ptab[i];
 }
 
-template <bool MIXED, int TE, bool RATES = false>
+template <bool MIXED, int TE, int MODE = kModePlanes>
 __device__ __forceinline__ void process_tile(const TileJob& j, int nl, int nl_pad, unsigned char* smem,
                                              const TileSmem& L) {
+    constexpr bool RATES = MODE == kModeRates;
     using Word = typename std::conditional<MIXED, int, double>::type;
     constexpr int W = MIXED ? kMixedWords : kFp64Words;
     Word* s_tab = (Word*)(smem + L.tab);
@@ -346,10 +363,15 @@ __device__ __forceinline__ void process_tile(const TileJob& j, int nl, int nl_pa
             MixedSrc<TE> src{(const int*)s_tab + lane, (const int*)s_pe + lane,
                              (const float2*)s_len_raw + (size_t)cl * nl_pad, s_ptab};
             const Q30 ar{};
-            Q30::C B[4];
-            flavour_block<Q30>(ar, src, M, B);
             float pr[9];
-            Q30::complete(B, pr);
+            if (MODE == kModeHeights) {
+                flavour_probs_heights<Q30>(ar, src, M, j.n_h, (const float2*)j.lenh + (size_t)ci * j.n_h,
+                                           (const float*)j.hw, pr);
+            } else {
+                Q30::C B[4];
+                flavour_block<Q30>(ar, src, M, B);
+                Q30::complete(B, pr);
+            }
             if (RATES) {
                 const int cb = ((const int*)(smem + L.cbin))[cl];
                 if (cb != run_cb) {
@@ -366,10 +388,15 @@ __device__ __forceinline__ void process_tile(const TileJob& j, int nl, int nl_pa
             F64Src<TE> src{(const double*)s_tab + lane, (const double*)s_pe + lane,
                            (const double*)s_len_raw + (size_t)cl * nl_pad};
             const F64 ar{};
-            F64::C B[4];
-            flavour_block<F64>(ar, src, M, B);
             double pr[9];
-            F64::complete(B, pr);
+            if (MODE == kModeHeights) {
+                flavour_probs_heights<F64>(ar, src, M, j.n_h, (const double*)j.lenh + (size_t)ci * j.n_h,
+                                           (const double*)j.hw, pr);
+            } else {
+                F64::C B[4];
+                flavour_block<F64>(ar, src, M, B);
+                F64::complete(B, pr);
+            }
             if (RATES) {
                 const int cb = ((const int*)(smem + L.cbin))[cl];
                 if (cb != run_cb) {

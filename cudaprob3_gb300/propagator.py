@@ -128,6 +128,16 @@ class CudaPropagatorSingle:
         check(self._lib.cp3_set_production_height(self._h, float(height_km)))
 
     # -- calculation (cudapropagator.cuh:162-235) -----------------------------
+    def setProductionHeights(self, heights_km, weights):
+        """Average the probabilities over production heights (km) with the
+        given weights (normalised); no reference counterpart (the reference
+        takes one height).  setProductionHeight ends the distribution."""
+        h = np.ascontiguousarray(heights_km, dtype=np.float64)
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        if h.shape != w.shape or h.ndim != 1:
+            raise ValueError("one weight per height")
+        check(self._lib.cp3_set_production_heights(self._h, _dptr(h), _dptr(w), int(h.size)))
+
     def calculateProbabilities(self, ntype):
         check(self._lib.cp3_calculate_probabilities(self._h, int(ntype)))
 

@@ -134,6 +134,17 @@ public:
     void setHostResultBuffer(FLOAT_T* host, size_t elements) {
         detail::check(cp3_set_host_result_buffer(alive(), host, elements * sizeof(FLOAT_T)));
     }
+    /// Production-height distribution (no reference counterpart): the
+    /// probabilities are averaged over the heights (km) with the weights
+    /// (normalised); setProductionHeight ends the distribution.
+    void setProductionHeights(const std::vector<FLOAT_T>& heightsKm, const std::vector<FLOAT_T>& weights) {
+        if (heightsKm.size() != weights.size())
+            throw std::runtime_error("setProductionHeights: one weight per height");
+        const auto h = detail::to_double(heightsKm), w = detail::to_double(weights);
+        detail::check(cp3_set_production_heights(alive(), h.data(), w.data(), (int)h.size()));
+        this->productionHeightKM = heightsKm.empty() ? FLOAT_T(0) : heightsKm[0];
+        this->isSetProductionHeight = true;
+    }
     /// Fused event rates (no reference counterpart): per-(cosine, energy)
     /// weights flux[3][n_cosines][n_energies] of the initial flavours (planes
     /// with a clear bit in flavourMask are not read), copied to the device.

@@ -100,6 +100,17 @@ int cp3_set_density_from_file(cp3_propagator* p, const char* path);
 /* Propagator::setProductionHeight, propagator.hpp:279-286 (km). */
 int cp3_set_production_height(cp3_propagator* p, double height_km);
 
+/* Production-height distribution (no reference counterpart: the reference
+ * takes one height, propagator.hpp:279-286).  Probabilities are averaged over
+ * the n heights (km, >= 0) with the given weights (>= 0, normalised here):
+ *   P(c, E) = sum_h w_h P(c, E; h).
+ * Only the atmosphere segment depends on the height, so the layer chain runs
+ * once per pair and each height adds one phase pair and a 2x3 by 3x2 product.
+ * n = 1 is cp3_set_production_height; cp3_set_production_height ends the
+ * distribution.  Fused rates are not available with a distribution. */
+#define CP3_MAX_HEIGHTS 64
+int cp3_set_production_heights(cp3_propagator* p, const double* heights_km, const double* weights, int n);
+
 /* CudaPropagatorSingle::calculateProbabilities, cudapropagator.cuh:162-165
  * (launch and wait).  type: CP3_NEUTRINO or CP3_ANTINEUTRINO. */
 int cp3_calculate_probabilities(cp3_propagator* p, int type);
