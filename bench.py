@@ -49,7 +49,8 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="target CPU time of the baseline sample")
     ap.add_argument("--skip-fp64", action="store_true")
-    ap.add_argument("--workload", choices=["grid4096", "batch", "precision", "gradient", "rates"], default="grid4096",
+    ap.add_argument("--workload", choices=["grid4096", "batch", "precision", "gradient", "rates", "heights"],
+                    default="grid4096",
                     help="grid4096: the headline line; batch: 1024 parameter sets with uneven grids in one "
                          "graph launch; precision: 64 parameter sets on the 8192 x 8192 grid")
     ap.add_argument("--sets", type=int, default=0, help="number of parameter sets (batch/precision)")
@@ -616,6 +617,93 @@ def run_rates(args, world, rank, local):
         p.close()
 
 
+def run_heights(args, world, rank, local):
+    """The 4096 x 4096 grid (nu + nubar per step) with probabilities averaged
+    over 8 production heights (10-45 km, weights of a broad hump): the chain
+    runs once per pair, each height adds a phase pair and a small product.
+    Reported beside the single-height time of the same grid, and checked
+    against the weighted average of the oracle at each height on a strided
+    subset."""
+    import torch
+
+    import cudaprob3_gb300 as cp
+    import oracle
+
+    torch.cuda.set_device(local)
+    dev = local
+    cos, en, B, nom = grid()
+    heights = np.array([10.0, 15.0, 20.0, 25.0, 30.0, 35.0, 40.0, 45.0])
+    weights = np.array([0.04, 0.10, 0.18, 0.22, 0.20, 0.14, 0.08, 0.04])
+    stream = torch.cuda.Stream(device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    props, bufs = [], []
+    for anti in (False, True):
+        p = make_prop(cp, "mixed", cos, en, B, nom, dev)
+        buf = torch.empty((9, NC, NE), dtype=torch.float32, device=dev)
+        p.set_result_buffer(buf.data_ptr(), buf.numel() * 4)
+        p.set_stream(stream.cuda_stream)
+        props.append((p, cp.Antineutrino if anti else cp.Neutrino))
+        bufs.append(buf)
+
+    def timed(steps, warmup):
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                for p, t in props:
+                    p.calculateProbabilitiesAsync(t)
+            stream.synchronize()
+            barrier(world)
+            evs = []
+            for _ in range(steps):
+                flush.zero_()
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                for p, t in props:
+                    p.calculateProbabilitiesAsync(t)
+                b.record(stream)
+                evs.append((a, b))
+            torch.cuda.synchronize()
+            barrier(world)
+        return allmax(world, float(np.mean([a.elapsed_time(b) for a, b in evs])))
+
+    single_ms = timed(max(3, min(args.steps, 20)), args.warmup)
+    for p, _ in props:
+        p.setProductionHeights(heights, weights)
+    sampler = ClockSampler(dev)
+    sampler.start()
+    ms = timed(args.steps, args.warmup)
+    clocks = sampler.stop()
+    # parity on a strided subset: every 64th cosine and energy
+    idx = np.arange(0, NC, 64)
+    err = 0.0
+    for (p, t), buf in zip(props, bufs):
+        p.calculateProbabilities(t)
+        got = buf.cpu().numpy()[:, idx][:, :, idx].astype(np.float64)
+        w = weights / weights.sum()
+        want = sum(wk * oracle.calculate(cos[idx], en[idx], B.radii, B.rho_eff(), nom, float(h),
+                                         t == cp.Antineutrino) for h, wk in zip(heights, w))
+        err = max(err, float(np.abs(got - want).max()))
+    pairs_step = 2 * NC * NE
+    if rank == 0:
+        line = {"metric": "(cos,E) pairs/s with probabilities averaged over 8 production heights (mixed)",
+                "value": world * pairs_step / (ms * 1e-3), "unit": "pairs/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "i32 Q1.30 chain + f32 phases + f64 eigen-solve, f32 height sums (float out)",
+                "data": "synthetic",
+                "config": {"workload": WORKLOAD + "; heights 10-45 km (8), weights " +
+                           ",".join("%.2f" % x for x in weights), "pairs_per_step": pairs_step,
+                           "l2": "flushed between steps (256 MB write outside the timed events)"},
+                "single_height": {"value": world * pairs_step / (single_ms * 1e-3), "ms_per_step": single_ms},
+                "cost_vs_single_height": ms / single_ms,
+                "gpu_launches": 2 * 2 * args.steps, "clocks": clocks,
+                "precision": {"max_abs_dp_vs_oracle_height_average_subset": err,
+                              "subset": "every 64th cosine x every 64th energy, nu and nubar"}}
+        print(json.dumps(line), flush=True)
+    for p, _ in props:
+        p.close()
+
+
 def run_precision(args, world, rank, local):
     import torch
 
@@ -762,6 +850,8 @@ def main():
             run_gradient(args, world, rank, local)
         elif args.workload == "rates":
             run_rates(args, world, rank, local)
+        elif args.workload == "heights":
+            run_heights(args, world, rank, local)
         else:
             run_ours(args, world, rank, local)
     finally:
