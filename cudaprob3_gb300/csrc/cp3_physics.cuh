@@ -31,12 +31,39 @@ namespace cp3 {
 // Lagrange projector (H - m_a)(H - m_b) for m_0 and m_1, and v_2 = v_0 x v_1,
 // which makes every basis right-handed (the propagation kernels rely on
 // det T_l = +1 for T_l = V_{l+1}^T V_l).
+//
+// FP64 divisions and square roots are long instruction sequences on GB300's
+// narrow FP64 pipe, so the solve avoids them where FP32 or a refinement
+// suffices: the trigonometric first guess is FP32 throughout; Newton steps
+// scale by an FP32 reciprocal of the derivative (the step error is then
+// quadratic plus 1e-7 times linear, below 1e-20 relative after two steps);
+// quotients use div_nr; normalisations use rsqrt.
+
+// a / b to about 1 ulp: FP32 reciprocal estimate refined by two Newton-Raphson
+// corrections of the quotient, q += r (a - q b) (each squares the relative
+// error: 1e-7 -> 1e-14 -> 1e-28).  |b| must lie in FP32's normal range.
+CP3_HD double div_nr(double a, double b) {
+    const double r = (double)(1.0f / (float)b);
+    double q = a * r;
+    q = fma(r, fma(-q, b, a), q);
+    q = fma(r, fma(-q, b, a), q);
+    return q;
+}
+
+CP3_HD double rsqrt_fp64(double x) {
+#ifdef __CUDA_ARCH__
+    return rsqrt(x);
+#else
+    return 1.0 / std::sqrt(x);
+#endif
+}
+
 CP3_HD double cubic_newton(double x, double a, double b, double g) {
 #pragma unroll
     for (int it = 0; it < 2; it++) {
         const double p = fma(fma(x + a, x, b), x, g);
         const double dp = fma(fma(3.0, x, 2.0 * a), x, b);
-        if (dp != 0.0) x -= p / dp;
+        if (dp != 0.0) x -= p * (double)(1.0f / (float)dp);
     }
     return x;
 }
@@ -63,8 +90,8 @@ CP3_HD void eigvec_of(const double H[9], double m, double ma, double mb, double 
         c1 = H[3] * H[2] + a4 * H[5] + H[5] * b8;
         c2 = n22;
     }
-    const double nrm = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
-    double inv = (nrm > 0.0) ? 1.0 / nrm : 0.0;
+    const double n2 = c0 * c0 + c1 * c1 + c2 * c2;
+    double inv = (n2 > 0.0) ? rsqrt_fp64(n2) : 0.0;
     // deterministic sign: largest component positive
     double big = c0;
     if (fabs(c1) > fabs(big)) big = c1;
@@ -81,19 +108,21 @@ CP3_HD void layer_eigen(const OscParams& p, double E, double rhoye, double m[3],
     const double a = fac + p.dm01 + p.dm02;
     const double b = p.dm01 * p.dm02 + fac * (p.dm01 * (1.0 - p.u01) + p.dm02 * (1.0 - p.u02));
     const double g = fac * p.dm01 * p.dm02 * p.u00;
-    // physics.hpp:298-324: trigonometric roots (first guess), then Newton
+    // physics.hpp:298-324: trigonometric roots as an FP32 first guess (the
+    // numerator and a^2 - 3b are formed in FP64: they cancel), then Newton
     double tmp = a * a - 3.0 * b;
     if (tmp < 0.0) tmp = 0.0;
-    const double sq = sqrt(tmp);
-    double arg = (2.0 * a * a * a - 9.0 * a * b + 27.0 * g) / (2.0 * sq * tmp);
-    if (!(fabs(arg) <= 1.0)) arg = (arg > 0.0) ? 1.0 : -1.0;
-    const float th = acosf((float)arg) * (1.0f / 3.0f);
+    const float tmpf = (float)tmp;
+    const float sqf = sqrtf(tmpf);
+    float arg = (float)(2.0 * a * a * a - 9.0 * a * b + 27.0 * g) / (2.0f * sqf * tmpf);
+    if (!(fabsf(arg) <= 1.0f)) arg = (arg > 0.0f) ? 1.0f : -1.0f;
+    const float th = acosf(arg) * (1.0f / 3.0f);
     float sf, cf;
     sincosf(th, &sf, &cf);
     const double c = cf, s = sf;
     const double h = 0.86602540378443864676;  // sin(2pi/3)
-    const double amp = -(2.0 / 3.0) * sq;
-    const double sh = -a / 3.0;
+    const double amp = -(2.0 / 3.0) * (double)sqf;
+    const double sh = a * (-1.0 / 3.0);
     {
     double q[3];
     q[0] = amp * c + sh;                   // cos(th)
@@ -113,11 +142,11 @@ CP3_HD void layer_eigen(const OscParams& p, double E, double rhoye, double m[3],
     const double qk = (rk == 0) ? q[0] : (rk == 1) ? q[1] : q[2];
     const double mi = cubic_newton(qi, a, b, g);
     const double S = -a - mi;
-    const double P = (fabs(mi) >= fabs(qj) && fabs(mi) >= fabs(qk) && mi != 0.0) ? -g / mi : b - mi * S;
+    const double P = (fabs(mi) >= fabs(qj) && fabs(mi) >= fabs(qk) && mi != 0.0) ? div_nr(-g, mi) : b - mi * S;
     double disc = S * S - 4.0 * P;
     if (disc < 0.0) disc = 0.0;
     const double big = 0.5 * (S + copysign(sqrt(disc), S));
-    const double small = (big != 0.0) ? P / big : 0.0;
+    const double small = (big != 0.0) ? div_nr(P, big) : 0.0;
     const double hi = fmax(big, small), lo = fmin(big, small);
     const double mj = (qj >= qk) ? hi : lo;
     const double mk = (qj >= qk) ? lo : hi;
@@ -161,8 +190,8 @@ CP3_HD void layer_eigen(const OscParams& p, double E, double rhoye, double m[3],
     vj[0] -= d * vi[0];
     vj[1] -= d * vi[1];
     vj[2] -= d * vi[2];
-    const double nj = sqrt(vj[0] * vj[0] + vj[1] * vj[1] + vj[2] * vj[2]);
-    const double rj = (nj > 0.0) ? 1.0 / nj : 0.0;
+    const double nj2 = vj[0] * vj[0] + vj[1] * vj[1] + vj[2] * vj[2];
+    const double rj = (nj2 > 0.0) ? rsqrt_fp64(nj2) : 0.0;
     vj[0] *= rj;
     vj[1] *= rj;
     vj[2] *= rj;
@@ -184,6 +213,10 @@ CP3_HD void layer_eigen(const OscParams& p, double E, double rhoye, double m[3],
 CP3_HD double phase_turns_per_km(double mk, double m0, double E) {
     return -kLoEfac * (mk - m0) / E / kTwoPi;
 }
+
+// The same with the energy factor -LoEfac / (2 pi E) computed once per
+// (energy, layer): phase_rate_factor(E) * (mk - m0).
+CP3_HD double phase_rate_factor(double E) { return -kLoEfac / (kTwoPi * E); }
 
 // Total path length including the production height (physics.hpp:615-616), cm.
 CP3_HD double path_length_cm(double c, double height_cm) {

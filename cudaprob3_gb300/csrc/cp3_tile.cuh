@@ -41,8 +41,9 @@ __device__ __forceinline__ void prep_energy_layer(const OscParams& osc, double E
     for (int w = 0; w < 9; w++) vme[w] = V[w];
     if (m_out)
         for (int k = 0; k < 3; k++) m_out[k] = m[k];
-    const double k1 = phase_turns_per_km(m[1], m[0], E);
-    const double k2 = phase_turns_per_km(m[2], m[0], E);
+    const double fE = phase_rate_factor(E);
+    const double k1 = (m[1] - m[0]) * fE;
+    const double k2 = (m[2] - m[0]) * fE;
     const size_t base = ((size_t)tile * g.nl + l) * W * te + lane;
     if (MIXED) {
         int* t = (int*)g.tab;

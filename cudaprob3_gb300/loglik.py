@@ -101,6 +101,12 @@ class BinnedProblem:
         lam = self.expected(pem, pmm)
         return float(np.sum(self.counts * np.log(lam) - lam))
 
+    def loglik_abs_sum(self, planes):
+        """sum_b |n_b ln(lambda_b)| + lambda_b for the nine planes [9][nc][ne]:
+        the scale of the rounding error of one log-likelihood evaluation."""
+        lam = self.expected(planes[1], planes[4])
+        return float(np.sum(np.abs(self.counts * np.log(lam)) + lam))
+
     def make(self, device_id=0, precision="fp64"):
         L = LogLikelihood(device_id, self.cosines.size, self.energies.size, precision)
         L.set_bins(self.cosines, self.energies)
