@@ -30,6 +30,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "cudaprob3_gb300.h"
@@ -114,8 +115,15 @@ struct LLArgs {
     double* pe;
     double* len;
     // partials and results
-    double* part_l;  // [n_cchunk][n_en][nl][11]
+    double* part_l;  // [n_cchunk][n_en][nl][11] (FP64 kernel)
     double* part_e;  // [n_cchunk][n_en][19]
+    float* part_l_f; // the same in float for the mixed kernel (null for FP64)
+    float* part_e_f;
+    // float copies of the inputs for the mixed kernel
+    const float* flux_e_f;
+    const float* flux_mu_f;
+    const float* counts_f;
+    float norm_f;
     double* part_g;  // [n_en][7 + n_rows]: per-energy LL and gradient
     double* out;     // [1 + 6 + nrows]: LL, gradient
     const int* layer_row;  // [nl]: caller's row of layer l (l >= 1), -1 for layer 0
@@ -338,20 +346,32 @@ __global__ void __launch_bounds__(128) ll_pair_kernel(LLArgs a) {
             B[1][b] = cjmul(Gb[0], g[0][b]) + cjmul(Gb[1], g[1][b]) + cjmul(Gb[2], g[2][b]);
         }
     }
-    // probabilities P(e -> mu) = |S[mu][e]|^2 = |B[1][0]|^2, P(mu -> mu) = |B[1][1]|^2
-    const double pem = (double)B[1][0].re * B[1][0].re + (double)B[1][0].im * B[1][0].im;
-    const double pmm = (double)B[1][1].re * B[1][1].re + (double)B[1][1].im * B[1][1].im;
-    double ll = 0.0;
+    // probabilities P(e -> mu) = |S[mu][e]|^2 = |B[1][0]|^2, P(mu -> mu) = |B[1][1]|^2;
+    // the bin's LL term and its seed in the kernel's precision (the mixed
+    // kernel holds no FP64 instruction in its loops)
+    const R pem = B[1][0].re * B[1][0].re + B[1][0].im * B[1][0].im;
+    const R pmm = B[1][1].re * B[1][1].re + B[1][1].im * B[1][1].im;
+    R ll = 0;
     R w_em = 0, w_mm = 0;
     if (valid) {
-        const double fe = a.flux_e[e], fm = a.flux_mu[e];
-        const double lam = a.norm * (fe * pem + fm * pmm);
-        const double n = a.counts[(size_t)c * a.n_en + e];
-        if (lam > 0.0) {
+        R fe, fm, n, nrm;
+        if constexpr (std::is_same<R, float>::value) {
+            fe = a.flux_e_f[e];
+            fm = a.flux_mu_f[e];
+            n = a.counts_f[(size_t)c * a.n_en + e];
+            nrm = a.norm_f;
+        } else {
+            fe = a.flux_e[e];
+            fm = a.flux_mu[e];
+            n = a.counts[(size_t)c * a.n_en + e];
+            nrm = a.norm;
+        }
+        const R lam = nrm * (fe * pem + fm * pmm);
+        if (lam > R(0)) {
             ll = n * log(lam) - lam;
-            const double w = (n / lam - 1.0) * a.norm;
-            w_em = (R)(w * fe);
-            w_mm = (R)(w * fm);
+            const R w = (n / lam - R(1)) * nrm;
+            w_em = w * fe;
+            w_mm = w * fm;
         } else {
             ll = -lam;
         }
@@ -446,7 +466,9 @@ __global__ void __launch_bounds__(128) ll_pair_kernel(LLArgs a) {
     }
 
     // per-(energy, layer) partials: layers Mw .. 1 (descending), then layer 0
-    double* pl = a.part_l + ((size_t)cchunk * a.n_en + e) * a.nl * kLLPerL;
+    // partials in the kernel's precision (float buffers for the mixed kernel)
+    R* pl = (R*)(std::is_same<R, float>::value ? (void*)a.part_l_f : (void*)a.part_l) +
+            ((size_t)cchunk * a.n_en + e) * a.nl * kLLPerL;
     for (int l = Mw; l >= 1; l--) {
         R tT[9];
         R tk[2] = {0, 0};
@@ -503,33 +525,34 @@ __global__ void __launch_bounds__(128) ll_pair_kernel(LLArgs a) {
 #pragma unroll
         for (int q = 0; q < 9; q++) {
             const R v = warp_sum(tT[q]);
-            if (lane == 0) pl[(size_t)l * kLLPerL + q] = (double)v;
+            if (lane == 0) pl[(size_t)l * kLLPerL + q] = v;
         }
 #pragma unroll
         for (int k = 0; k < 2; k++) {
             const R v = warp_sum(tk[k]);
-            if (lane == 0) pl[(size_t)l * kLLPerL + 9 + k] = (double)v;
+            if (lane == 0) pl[(size_t)l * kLLPerL + 9 + k] = v;
         }
     }
     // layers above Mw are never crossed by this warp's cosines
     if (lane == 0)
         for (int l = Mw + 1; l < a.nl; l++)
-            for (int q = 0; q < kLLPerL; q++) pl[(size_t)l * kLLPerL + q] = 0.0;
+            for (int q = 0; q < kLLPerL; q++) pl[(size_t)l * kLLPerL + q] = R(0);
     // layer 0: T_0 and D_0
     {
 #pragma unroll
         for (int q = 0; q < 9; q++) {
             const R v = warp_sum(gT0[q / 3][q % 3]);
-            if (lane == 0) pl[q] = (double)v;
+            if (lane == 0) pl[q] = v;
         }
 #pragma unroll
         for (int k = 1; k < 3; k++) {
             const R v = warp_sum(-twopi * src.L(0) * cjmul(gD0[k], D0[k]).im);
-            if (lane == 0) pl[9 + k - 1] = (double)v;
+            if (lane == 0) pl[9 + k - 1] = v;
         }
     }
-    // per energy: Lambda', Gamma' (kernel precision), LL (FP64)
-    double* pe = a.part_e + ((size_t)cchunk * a.n_en + e) * kLLPerE;
+    // per energy: Lambda', Gamma', LL
+    R* pe = (R*)(std::is_same<R, float>::value ? (void*)a.part_e_f : (void*)a.part_e) +
+            ((size_t)cchunk * a.n_en + e) * kLLPerE;
     R vals[kLLPerE - 1];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
@@ -543,9 +566,9 @@ __global__ void __launch_bounds__(128) ll_pair_kernel(LLArgs a) {
 #pragma unroll
     for (int q = 0; q < kLLPerE - 1; q++) {
         const R v = warp_sum(vals[q]);
-        if (lane == 0) pe[q] = (double)v;
+        if (lane == 0) pe[q] = v;
     }
-    const double llw = warp_sum(ll);
+    const R llw = warp_sum(ll);
     if (lane == 0) pe[kLLPerE - 1] = llw;
 }
 
@@ -554,32 +577,53 @@ __global__ void __launch_bounds__(128) ll_pair_kernel(LLArgs a) {
 // theta23, dCP, dm12sq, dm23sq, [7 + r] density of the caller's row r.
 constexpr int kLLOscOut = 7;
 
-// Block e, thread l < nl: layer l of energy e.  The thread sums the warps'
-// partials of its layer, re-solves the layer's eigen-problem in FP64, takes
-// the adjoint of its eigenvectors from the two overlaps it enters
-// (T_{l-1} = V_l^T V_{l-1} and T_l = V_{l+1}^T V_l, neighbours through shared
-// memory) and back-propagates through the eigen-decomposition to the
+// Lanes per energy in ll_layer_kernel: 8 or 16 when the layers fit (2 or 4
+// energies share a warp), else a multiple of 32.
+__host__ __device__ inline int ll_layer_lanes(int nl) { return nl <= 8 ? 8 : nl <= 16 ? 16 : (nl + 31) / 32 * 32; }
+
+// Energy slot s of block b is energy b * EPB + s (EPB = blockDim.x / S, S =
+// ll_layer_lanes); its thread l < nl handles layer l.  The thread sums the
+// warps' partials of its layer, takes the layer's FP64 eigen-pairs from the
+// prep kernel, the adjoint of its eigenvectors from the two overlaps it
+// enters (T_{l-1} = V_l^T V_{l-1} and T_l = V_{l+1}^T V_l, neighbours through
+// shared memory) and back-propagates through the eigen-decomposition to the
 // parameters.  The rows of the body map one-to-one to layers 1..nl-1, so each
 // density slot has a single writer; the oscillation parameters are summed
-// over the block in a fixed order.
+// over the energy's lanes in a fixed order.
 __global__ void __launch_bounds__(96) ll_layer_kernel(LLArgs a) {
-    __shared__ double sV[kMaxRows + 1][9];
-    __shared__ double sT[kMaxRows + 1][9];
-    __shared__ double sL[kLLPerE];
-    __shared__ double sRed[3][kLLOscOut];
-    const int e = blockIdx.x, l = threadIdx.x, nl = a.nl;
+    extern __shared__ double s_ll[];
+    const int nl = a.nl, S = ll_layer_lanes(nl), EPB = max(1, (int)blockDim.x / S);
+    const int slot = threadIdx.x / S, l = threadIdx.x % S;
+    const int e = blockIdx.x * EPB + slot;
+    const bool live_e = e < a.n_en;
+    double* sV = s_ll + (size_t)slot * nl * 9;                   // [EPB][nl][9]
+    double* sT = s_ll + (size_t)EPB * nl * 9 + (size_t)slot * nl * 9;
+    double* sL = s_ll + (size_t)2 * EPB * nl * 9 + (size_t)slot * kLLPerE;
+    double* sRed = s_ll + (size_t)2 * EPB * nl * 9 + (size_t)EPB * kLLPerE;  // [blockDim/32][7]
     const OscParams& o = *a.osc;
-    const double E = a.energies[e];
+    const double E = live_e ? a.energies[e] : 1.0;
     double gT[9], gK0 = 0.0, gK1 = 0.0, m[3], V[9];
 #pragma unroll
     for (int q = 0; q < 9; q++) gT[q] = 0.0;
-    if (l < nl) {
-        for (int cc = 0; cc < a.n_cchunk; cc++) {
-            const double* pl = a.part_l + (((size_t)cc * a.n_en + e) * nl + l) * kLLPerL;
+    const bool live = live_e && l < nl;
+    if (live) {
+        // the warps' partials (float from the mixed pair kernel), summed in FP64
+        if (a.part_l_f) {
+            for (int cc = 0; cc < a.n_cchunk; cc++) {
+                const float* pl = a.part_l_f + (((size_t)cc * a.n_en + e) * nl + l) * kLLPerL;
 #pragma unroll
-            for (int q = 0; q < 9; q++) gT[q] += pl[q];
-            gK0 += pl[9];
-            gK1 += pl[10];
+                for (int q = 0; q < 9; q++) gT[q] += (double)pl[q];
+                gK0 += (double)pl[9];
+                gK1 += (double)pl[10];
+            }
+        } else {
+            for (int cc = 0; cc < a.n_cchunk; cc++) {
+                const double* pl = a.part_l + (((size_t)cc * a.n_en + e) * nl + l) * kLLPerL;
+#pragma unroll
+                for (int q = 0; q < 9; q++) gT[q] += pl[q];
+                gK0 += pl[9];
+                gK1 += pl[10];
+            }
         }
         // eigen-pairs of this (energy, layer) as solved by the prep kernel
         const double* ev = a.eig + ((size_t)e * nl + l) * kLLEigWords;
@@ -589,23 +633,27 @@ __global__ void __launch_bounds__(96) ll_layer_kernel(LLArgs a) {
         for (int k = 0; k < 3; k++) m[k] = ev[9 + k];
 #pragma unroll
         for (int q = 0; q < 9; q++) {
-            sV[l][q] = V[q];
-            sT[l][q] = gT[q];
+            sV[l * 9 + q] = V[q];
+            sT[l * 9 + q] = gT[q];
         }
     }
-    if (l < kLLPerE) {
-        double v = 0.0;
-        for (int cc = 0; cc < a.n_cchunk; cc++) v += a.part_e[((size_t)cc * a.n_en + e) * kLLPerE + l];
-        sL[l] = v;
-    }
+    if (live_e)
+        for (int w = l; w < kLLPerE; w += S) {
+            double v = 0.0;
+            for (int cc = 0; cc < a.n_cchunk; cc++) {
+                const size_t i = ((size_t)cc * a.n_en + e) * kLLPerE + w;
+                v += a.part_e_f ? (double)a.part_e_f[i] : a.part_e[i];
+            }
+            sL[w] = v;
+        }
     __syncthreads();
 
     double acc[kLLOscOut];
 #pragma unroll
     for (int q = 0; q < kLLOscOut; q++) acc[q] = 0.0;
     const int np = 6 + a.n_rows;
-    double* grow = a.part_g + (size_t)e * (1 + np);
-    if (l < nl) {
+    double* grow = a.part_g + (size_t)(live_e ? e : 0) * (1 + np);
+    if (live) {
         const double s23 = o.s23, c23 = o.c23, sd = o.sd, cd = o.cd;
         double gV[9];
 #pragma unroll
@@ -617,7 +665,7 @@ __global__ void __launch_bounds__(96) ll_layer_kernel(LLArgs a) {
 #pragma unroll
                 for (int j = 0; j < 3; j++)
 #pragma unroll
-                    for (int r = 0; r < 3; r++) gV[3 * r + j] += sT[l][3 * i + j] * sV[l + 1][3 * r + i];
+                    for (int r = 0; r < 3; r++) gV[3 * r + j] += sT[l * 9 + 3 * i + j] * sV[(l + 1) * 9 + 3 * r + i];
         }
         // T_{l-1} = V_l^T V_{l-1}: dT_{l-1}[i][j] / dV_l[r][i] = V_{l-1}[r][j]
         if (l >= 1) {
@@ -626,7 +674,8 @@ __global__ void __launch_bounds__(96) ll_layer_kernel(LLArgs a) {
 #pragma unroll
                 for (int j = 0; j < 3; j++)
 #pragma unroll
-                    for (int r = 0; r < 3; r++) gV[3 * r + i] += sT[l - 1][3 * i + j] * sV[l - 1][3 * r + j];
+                    for (int r = 0; r < 3; r++)
+                        gV[3 * r + i] += sT[(l - 1) * 9 + 3 * i + j] * sV[(l - 1) * 9 + 3 * r + j];
         }
         if (l == 1) {
             // Lambda' from V_1: row 0 = V_1[0][k]; row 1 = c23 V_1[1][k] + s23 e^{i d} V_1[2][k]
@@ -663,7 +712,7 @@ __global__ void __launch_bounds__(96) ll_layer_kernel(LLArgs a) {
         const double dO12[9] = {-c13 * sn12, c13 * c12, 0.0, -c12, -sn12, 0.0, s13 * sn12, -s13 * c12, 0.0};
         const double dO13[9] = {-s13 * c12, -s13 * sn12, c13, 0.0, 0.0, 0.0, -c13 * c12, -c13 * sn12, -s13};
         // dLL/dm_k from the phase rates kappa_k = -LoE (m_k - m_0) / (2 pi E), k = 1, 2
-        const double f = -kLoEfac / (kTwoPi * E);
+        const double f = phase_rate_factor(E);
         const double gm[3] = {-(gK0 + gK1) * f, gK0 * f, gK1 * f};
         // gH = sum_k gm_k v_k v_k^T + sum_{k != j} (v_j . gv_k) / (m_k - m_j) v_j v_k^T
         double W[3][3];  // W[j][k] = coefficient of v_j v_k^T
@@ -686,19 +735,19 @@ __global__ void __launch_bounds__(96) ll_layer_kernel(LLArgs a) {
         for (int p = 0; p < 3; p++)
 #pragma unroll
             for (int q = 0; q < 3; q++) {
-                double s = 0.0;
+                double sum = 0.0;
 #pragma unroll
                 for (int j = 0; j < 3; j++)
 #pragma unroll
-                    for (int k = 0; k < 3; k++) s += W[j][k] * V[3 * p + j] * V[3 * q + k];
-                gH[p][q] = s;
+                    for (int k = 0; k < 3; k++) sum += W[j][k] * V[3 * p + j] * V[3 * q + k];
+                gH[p][q] = sum;
             }
 #pragma unroll
         for (int p = 0; p < 3; p++)
 #pragma unroll
             for (int q = p + 1; q < 3; q++) {
-                const double s = 0.5 * (gH[p][q] + gH[q][p]);
-                gH[p][q] = gH[q][p] = s;
+                const double sym = 0.5 * (gH[p][q] + gH[q][p]);
+                gH[p][q] = gH[q][p] = sym;
             }
         double gd1 = 0.0, gd2 = 0.0, gth12 = 0.0, gth13 = 0.0;
         const double dd[3] = {0.0, o.d1, o.d2};
@@ -727,18 +776,30 @@ __global__ void __launch_bounds__(96) ll_layer_kernel(LLArgs a) {
             grow[1 + 6 + a.layer_row[l]] = -gH[0][0] * sgn * kGF * E * a.ye_layer[l];
         }
     }
-    // fixed-order block sum of the oscillation slots
-    const int w = l >> 5, lane = l & 31;
+    // fixed-order sum of the oscillation slots over the energy's lanes:
+    // butterflies inside S-lane segments (S <= 32), then across warps
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int width = S < 32 ? S : 32;
 #pragma unroll
     for (int q = 0; q < kLLOscOut; q++) {
-        const double v = warp_sum(acc[q]);
-        if (lane == 0) sRed[w][q] = v;
+        double v = acc[q];
+        for (int off = width >> 1; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        acc[q] = v;
     }
-    __syncthreads();
-    if (l < kLLOscOut) {
-        double v = 0.0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); i++) v += sRed[i][l];
-        grow[l] = v;
+    if (S <= 32) {
+        if (l == 0 && live_e)
+#pragma unroll
+            for (int q = 0; q < kLLOscOut; q++) grow[q] = acc[q];
+    } else {
+        if (lane == 0)
+#pragma unroll
+            for (int q = 0; q < kLLOscOut; q++) sRed[w * kLLOscOut + q] = acc[q];
+        __syncthreads();
+        if ((int)threadIdx.x < kLLOscOut && live_e) {
+            double v = 0.0;
+            for (int i = 0; i < (int)(blockDim.x >> 5); i++) v += sRed[i * kLLOscOut + threadIdx.x];
+            grow[threadIdx.x] = v;
+        }
     }
 }
 
@@ -799,6 +860,7 @@ struct cp3_loglik {
     double *d_en = nullptr, *d_cos = nullptr, *d_radii = nullptr, *d_fe = nullptr, *d_fm = nullptr, *d_counts = nullptr;
     double *d_tab = nullptr, *d_pe = nullptr, *d_len = nullptr, *d_pl = nullptr, *d_pee = nullptr, *d_out = nullptr;
     double* d_pg = nullptr;
+    float *d_plf = nullptr, *d_peef = nullptr, *d_fef = nullptr, *d_fmf = nullptr, *d_cntf = nullptr;
     double* d_eig = nullptr;
     float *d_tabf = nullptr, *d_pef = nullptr;
     float2* d_lenf = nullptr;
@@ -822,7 +884,7 @@ void ll_free(cp3_loglik* L) {
     L->graph = nullptr;
     void* ptrs[] = {L->d_en, L->d_cos, L->d_radii, L->d_fe, L->d_fm, L->d_counts, L->d_tab, L->d_pe, L->d_len,
                     L->d_pl, L->d_pee, L->d_out, L->d_pg, L->d_rhoye, L->d_yel, L->d_maxl, L->d_row, L->d_osc,
-                    L->d_eig, L->d_tabf, L->d_pef, L->d_lenf};
+                    L->d_eig, L->d_tabf, L->d_pef, L->d_lenf, L->d_plf, L->d_peef, L->d_fef, L->d_fmf, L->d_cntf};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     L->d_en = L->d_cos = L->d_radii = L->d_fe = L->d_fm = L->d_counts = nullptr;
@@ -830,6 +892,7 @@ void ll_free(cp3_loglik* L) {
     L->d_eig = nullptr;
     L->d_tabf = L->d_pef = nullptr;
     L->d_lenf = nullptr;
+    L->d_plf = L->d_peef = L->d_fef = L->d_fmf = L->d_cntf = nullptr;
     L->d_maxl = L->d_row = nullptr;
     L->d_osc = nullptr;
 }
@@ -873,6 +936,12 @@ cp3::LLArgs ll_args(cp3_loglik* L, int type) {
     a.tabf = L->mixed ? L->d_tabf : nullptr;
     a.pef = L->mixed ? L->d_pef : nullptr;
     a.lenf = L->mixed ? L->d_lenf : nullptr;
+    a.part_l_f = L->mixed ? L->d_plf : nullptr;
+    a.part_e_f = L->mixed ? L->d_peef : nullptr;
+    a.flux_e_f = L->d_fef;
+    a.flux_mu_f = L->d_fmf;
+    a.counts_f = L->d_cntf;
+    a.norm_f = (float)L->norm;
     a.out = L->d_out;
     a.layer_row = L->d_row;
     a.n_rows = L->n_rows;
@@ -914,6 +983,14 @@ int ll_setup(cp3_loglik* L, int type) {
         (e = cudaMalloc((void**)&L->d_osc, sizeof(cp3::OscParams))) ||
         (e = cudaMalloc(&L->d_eig, (size_t)L->n_en_pad * L->nl * cp3::kLLEigWords * 8)))
         return lcuda(e, "cudaMalloc(loglik)");
+    if (L->mixed) {
+        std::vector<float> fe(L->flux_e.begin(), L->flux_e.end()), fm(L->flux_mu.begin(), L->flux_mu.end());
+        std::vector<float> cnt(L->counts.begin(), L->counts.end());
+        if ((e = dmalloc_copy(&L->d_fef, fe.data(), fe.size())) || (e = dmalloc_copy(&L->d_fmf, fm.data(), fm.size())) ||
+            (e = dmalloc_copy(&L->d_cntf, cnt.data(), cnt.size())) || (e = cudaMalloc(&L->d_plf, pl * 4)) ||
+            (e = cudaMalloc(&L->d_peef, pee * 4)))
+            return lcuda(e, "cudaMalloc(loglik)");
+    }
     if (L->mixed &&
         ((e = cudaMalloc(&L->d_tabf, (size_t)L->n_en_pad * L->nl * cp3::kLLFWords * 4)) ||
          (e = cudaMalloc(&L->d_pef, (size_t)18 * L->n_en_pad * 4)) || (e = cudaMalloc(&L->d_lenf, len * 8))))
@@ -931,7 +1008,7 @@ int ll_setup(cp3_loglik* L, int type) {
         // eigen-solves over the GPU (about two per SM), at most 256 threads
         int sms = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, L->device);
-        const int eb = std::max(1, std::min(256 / L->nl, L->n_en_pad / std::max(1, 2 * sms)));
+        const int eb = std::max(1, std::min(256 / L->nl, std::max(32 / L->nl, L->n_en_pad / std::max(1, 2 * sms))));
         const int nbE = (L->n_en_pad + eb - 1) / eb;
         const int nbC = (L->n_cos + L->nl * eb - 1) / (L->nl * eb);
         cp3::ll_prep_kernel<<<nbE + nbC, dim3(L->nl, eb), (size_t)eb * L->nl * 9 * 8, cs>>>(a);
@@ -946,7 +1023,9 @@ int ll_setup(cp3_loglik* L, int type) {
         e = cudaGetLastError();
     }
     if (!e) {
-        cp3::ll_layer_kernel<<<L->n_en, (L->nl + 31) / 32 * 32, 0, cs>>>(a);
+        const int S = cp3::ll_layer_lanes(L->nl), epb = std::max(1, 32 / S), threads = epb * S;
+        const size_t smem = ((size_t)2 * epb * L->nl * 9 + (size_t)epb * cp3::kLLPerE + (size_t)(threads / 32) * 7) * 8;
+        cp3::ll_layer_kernel<<<(L->n_en + epb - 1) / epb, threads, smem, cs>>>(a);
         e = cudaGetLastError();
     }
     if (!e) {

@@ -2,13 +2,14 @@
 
     python -m cudaprob3_gb300.profile_case [--n 2048] [--precision mixed|fp64]
                                            [--repeat 1] [--anti]
-                                           [--mode planes|rates|heights]
+                                           [--mode planes|rates|heights|gradient]
 
 Grid: n cosines in [-1, 0] x n energies log-spaced over 0.1-1000 GeV on the
 11-shell PREM body at the nominal parameters.  Modes: the nine planes; fused
 event rates into 400 x 200 bins (flux E^-2.7, nu_e = nu_mu/2); planes
-averaged over 8 production heights (10-45 km).  Prints the wall time of the
-repeated calculations.
+averaged over 8 production heights (10-45 km); gradient: evaluations of the
+400 x 200 binned log-likelihood and its adjoint gradient (the n option does
+not apply).  Prints the wall time of the repeated calculations.
 """
 import argparse
 import time
@@ -25,8 +26,20 @@ def main():
     ap.add_argument("--precision", default="mixed")
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--anti", action="store_true")
-    ap.add_argument("--mode", default="planes", choices=["planes", "rates", "heights"])
+    ap.add_argument("--mode", default="planes", choices=["planes", "rates", "heights", "gradient"])
     a = ap.parse_args()
+    if a.mode == "gradient":
+        from .loglik import binned_problem
+        prob = binned_problem(device_id=0)
+        L = prob.make(device_id=0, precision=a.precision)
+        L.evaluate(prob.nominal, prob.body.rhos)
+        t0 = time.perf_counter()
+        for _ in range(a.repeat):
+            L.evaluate(prob.nominal, prob.body.rhos)
+        dt = time.perf_counter() - t0
+        L.close()
+        print("gradient precision=%s repeat=%d: %.3f ms per evaluation" % (a.precision, a.repeat, 1e3 * dt / a.repeat))
+        return
     c = G.linspace(-1.0, 0.0, a.n)
     e = G.logspace(0.1, 1000.0, a.n)
     B = G.PREM_12
