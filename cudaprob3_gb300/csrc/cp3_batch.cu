@@ -278,6 +278,11 @@ struct cp3_batch {
     std::vector<cp3::BatchGrid> grids;
     std::vector<int2> eblk, cblk;
     std::vector<int4> items;
+    // the sets are split into chunks of about equal work: chunk k's prep runs
+    // while the persistent kernel propagates chunk k - 1 (offsets into the
+    // lists above, n_chunks + 1 entries each)
+    int n_chunks = 0;
+    std::vector<int> chunk_eblk, chunk_cblk, chunk_items;
     int nl = 0, nl_pad = 0, eb = 1, blocks = 0;
     size_t smem = 0;
 
@@ -312,14 +317,45 @@ int build_layout(cp3_batch* b) {
     b->nl = n + 1;
     b->nl_pad = (b->nl + 1) / 2 * 2;
     const int W = b->mixed ? cp3::kMixedWords : cp3::kFp64Words;
-    b->eb = std::max(1, 256 / b->nl);
+    // one-warp prep blocks: they run beside the persistent propagate blocks,
+    // in the registers those leave free (3 x 256 threads x 80 registers of
+    // 65,536 leave room for one warp)
+    b->eb = std::max(1, 32 / b->nl);
     b->grids.assign(b->n_sets, cp3::BatchGrid{});
     b->eblk.clear();
     b->cblk.clear();
     b->items.clear();
+    b->chunk_eblk.assign(1, 0);
+    b->chunk_cblk.assign(1, 0);
+    b->chunk_items.assign(1, 0);
     long long tab = 0, pe = 0, len = 0;
     const int cthreads = b->nl * b->eb;
+    // work of every set (the chain cost of its cosines times its energy tiles)
+    std::vector<double> set_cost(b->n_sets, 0.0);
+    double total_cost = 0.0;
+    int live_sets = 0;
+    for (int s = 0; s < b->n_sets; s++) {
+        if (b->n_cos[s] == 0 || b->n_en[s] == 0) continue;
+        double c = 0.0;
+        for (int i = 0; i < b->n_cos[s]; i++) c += 78.0 * b->maxl[b->cos_off[s] + i] + 116.0;
+        set_cost[s] = c * ((b->n_en[s] + b->te - 1) / b->te);
+        total_cost += set_cost[s];
+        live_sets++;
+    }
+    const int K = std::max(1, std::min(8, live_sets));
     std::vector<std::pair<double, int4>> work;
+    double done = 0.0;
+    int chunk = 0;
+    auto close_chunk = [&]() {
+        std::stable_sort(work.begin(), work.end(),
+                         [](const std::pair<double, int4>& x, const std::pair<double, int4>& y) { return x.first > y.first; });
+        for (auto& w : work) b->items.push_back(w.second);
+        work.clear();
+        b->chunk_eblk.push_back((int)b->eblk.size());
+        b->chunk_cblk.push_back((int)b->cblk.size());
+        b->chunk_items.push_back((int)b->items.size());
+        chunk++;
+    };
     for (int s = 0; s < b->n_sets; s++) {
         cp3::BatchGrid& g = b->grids[s];
         g.n_cos = b->n_cos[s];
@@ -345,11 +381,11 @@ int build_layout(cp3_batch* b) {
                 for (int c = c0; c < c0 + ncl; c++) cost += 78.0 * b->maxl[g.cos_off + c] + 116.0;
                 work.push_back({cost, make_int4(s, t, c0, ncl)});
             }
+        done += set_cost[s];
+        if (chunk < K - 1 && done >= total_cost * (chunk + 1) / K) close_chunk();
     }
-    std::stable_sort(work.begin(), work.end(), [](const std::pair<double, int4>& x, const std::pair<double, int4>& y) {
-        return x.first > y.first;
-    });
-    for (auto& w : work) b->items.push_back(w.second);
+    close_chunk();
+    b->n_chunks = chunk;
     const size_t word = b->mixed ? 4 : 8;
     cudaError_t e;
     if ((e = b->d_tab.ensure((size_t)tab * word)) != cudaSuccess) return bcuda(e, "cudaMalloc(tables)");
@@ -359,6 +395,7 @@ int build_layout(cp3_batch* b) {
     if ((e = b->d_eblk.ensure(b->eblk.size())) != cudaSuccess) return bcuda(e, "cudaMalloc");
     if ((e = b->d_cblk.ensure(b->cblk.size())) != cudaSuccess) return bcuda(e, "cudaMalloc");
     if ((e = b->d_items.ensure(b->items.size())) != cudaSuccess) return bcuda(e, "cudaMalloc");
+    if ((e = b->d_counter.ensure(std::max(1, b->n_chunks))) != cudaSuccess) return bcuda(e, "cudaMalloc");
     if (!b->eblk.empty() &&
         (e = cudaMemcpy(b->d_eblk.p, b->eblk.data(), b->eblk.size() * sizeof(int2), cudaMemcpyHostToDevice)))
         return bcuda(e, "cudaMemcpy");
@@ -377,7 +414,7 @@ int build_layout(cp3_batch* b) {
     if (bps < 1) return bfail(CP3_ERR_LIMIT, "batch: launch shape does not fit on an SM");
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
-    b->blocks = std::max(1, std::min<int>(sms * bps, (int)b->items.size()));
+    b->blocks = std::max(1, sms * bps);  // per chunk: at most its item count
     b->layout_dirty = false;
     b->desc_dirty = true;
     drop_graph(b);
@@ -441,13 +478,13 @@ int upload_inputs(cp3_batch* b) {
     return CP3_OK;
 }
 
-cp3::BatchPrepArgs prep_args(cp3_batch* b) {
+cp3::BatchPrepArgs prep_args(cp3_batch* b, int k) {
     cp3::BatchPrepArgs a{};
     a.grids = b->d_grids.p;
-    a.eblk = b->d_eblk.p;
-    a.cblk = b->d_cblk.p;
-    a.n_eblk = (int)b->eblk.size();
-    a.n_cblk = (int)b->cblk.size();
+    a.eblk = b->d_eblk.p + b->chunk_eblk[k];
+    a.cblk = b->d_cblk.p + b->chunk_cblk[k];
+    a.n_eblk = b->chunk_eblk[k + 1] - b->chunk_eblk[k];
+    a.n_cblk = b->chunk_cblk[k + 1] - b->chunk_cblk[k];
     a.eb = b->eb;
     a.energies = b->d_en.p;
     a.cosines = b->d_cos.p;
@@ -464,12 +501,12 @@ cp3::BatchPrepArgs prep_args(cp3_batch* b) {
     return a;
 }
 
-cp3::BatchPropArgs prop_args(cp3_batch* b) {
+cp3::BatchPropArgs prop_args(cp3_batch* b, int k) {
     cp3::BatchPropArgs a{};
     a.grids = b->d_grids.p;
-    a.items = b->d_items.p;
-    a.n_items = (int)b->items.size();
-    a.counter = b->d_counter.p;
+    a.items = b->d_items.p + b->chunk_items[k];
+    a.n_items = b->chunk_items[k + 1] - b->chunk_items[k];
+    a.counter = b->d_counter.p + k;
     a.tab = b->d_tab.p;
     a.pe = b->d_pe.p;
     a.len = b->d_len.p;
@@ -482,19 +519,46 @@ cp3::BatchPropArgs prop_args(cp3_batch* b) {
     return a;
 }
 
-// Capture: counter reset, prep, persistent propagate.
+// Capture: counter reset, then per chunk k a prep launch on a side stream and
+// the persistent propagate of chunk k on the main stream after it, so that
+// chunk k + 1's FP64 prep overlaps chunk k's propagation.
 int capture(cp3_batch* b) {
     drop_graph(b);
-    cudaStream_t cs;
+    const int K = b->n_chunks;
+    cudaStream_t cs = nullptr, side = nullptr;
+    std::vector<cudaEvent_t> evs(K + 1, nullptr);
     cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
-    if (e) return bcuda(e, "cudaStreamCreate");
+    if (!e) e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
+    for (int k = 0; k <= K && !e; k++) e = cudaEventCreateWithFlags(&evs[k], cudaEventDisableTiming);
+    auto cleanup = [&]() {
+        for (cudaEvent_t ev : evs)
+            if (ev) cudaEventDestroy(ev);
+        if (side) cudaStreamDestroy(side);
+        if (cs) cudaStreamDestroy(cs);
+    };
+    if (e) {
+        cleanup();
+        return bcuda(e, "graph capture set-up");
+    }
     e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-    if (!e) e = cudaMemsetAsync(b->d_counter.p, 0, sizeof(int), cs);
-    if (!e) e = cp3::batch_prep_launch(b->mixed, prep_args(b), cs);
-    if (!e && !b->items.empty()) e = cp3::batch_launch(b->mixed, b->te, prop_args(b), b->groups, b->smem, b->blocks, cs);
+    bool capturing = !e;
+    if (!e) e = cudaMemsetAsync(b->d_counter.p, 0, sizeof(int) * std::max(1, K), cs);
+    if (!e) e = cudaEventRecord(evs[K], cs);  // fork
+    if (!e) e = cudaStreamWaitEvent(side, evs[K], 0);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+    for (int k = 0; k < K && !e; k++) {
+        e = cp3::batch_prep_launch(b->mixed, prep_args(b, k), side);
+        if (!e) e = cudaEventRecord(evs[k], side);
+        if (!e) e = cudaStreamWaitEvent(cs, evs[k], 0);  // joins the side stream at the last chunk
+        const int n_items = b->chunk_items[k + 1] - b->chunk_items[k];
+        if (!e && n_items > 0)
+            e = cp3::batch_launch(b->mixed, b->te, prop_args(b, k), b->groups, b->smem, std::min(b->blocks, n_items),
+                                  cs);
+    }
     cudaGraph_t g = nullptr;
-    cudaError_t e2 = cudaStreamEndCapture(cs, &g);
-    cudaStreamDestroy(cs);
+    cudaError_t e2 = capturing ? cudaStreamEndCapture(cs, &g) : cudaSuccess;
+    cleanup();
     if (e || e2) {
         if (g) cudaGraphDestroy(g);
         return bcuda(e ? e : e2, "graph capture");
