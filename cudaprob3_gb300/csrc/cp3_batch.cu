@@ -103,7 +103,7 @@ struct BatchPropArgs {
 };
 
 template <bool MIXED, int TE>
-__global__ void __launch_bounds__(MIXED ? 256 : 128, 3) batch_propagate_kernel(BatchPropArgs a) {
+__global__ void __launch_bounds__(MIXED ? 256 : 128, MIXED ? 4 : 3) batch_propagate_kernel(BatchPropArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const TileSmem L = tile_smem(MIXED, TE, a.nl, a.nl_pad, a.cchunk);
     int& s_item = *(int*)(smem + L.total);  // work-item slot after the tile (all shared memory is dynamic)

@@ -101,8 +101,12 @@ template <class P, class Src>
 __device__ __forceinline__ void flavour_block(const P& ar, const Src& src, int M, typename P::C B[4]) {
     using R = typename P::R;
     using C = typename P::C;
-    R c1, s1, n1, c2, s2, n2;
+    // G = Y^T D_M Y first: nothing of the atmosphere segment is live during
+    // the layer chain (fewer registers across the loop)
+    C G[6];  // 00 01 02 11 12 22
+    if (M > 0) chain_G(ar, src, M, G);
     // X' = T_0 D_0 Gamma' (3x2), or D_0 Gamma' when only the atmosphere is crossed
+    R c1, s1, n1, c2, s2, n2;
     src.phase(0, c1, s1, n1, c2, s2, n2);
     C g0[3], g1[3];  // D_0 Gamma': columns 0 and 1
     g0[0] = P::creal(src.Ga(0));
@@ -127,8 +131,6 @@ __device__ __forceinline__ void flavour_block(const P& ar, const Src& src, int M
         x0[i] = ar.dotRC(src.T(0, i, 0), src.T(0, i, 1), src.T(0, i, 2), g0[0], g0[1], g0[2]);
         x1[i] = ar.dotRC(src.T(0, i, 0), src.T(0, i, 1), src.T(0, i, 2), g1[0], g1[1], g1[2]);
     }
-    C G[6];  // Y^T D_M Y: 00 01 02 11 12 22
-    chain_G(ar, src, M, G);
     // X = G X' (3x2)
     C X0[3], X1[3];
     X0[0] = ar.dotCC(G[0], G[1], G[2], x0[0], x0[1], x0[2]);

@@ -70,8 +70,12 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a) {
 }
 
 // ------------------------------------------------------------ propagate ----
+// Mixed planes and rates: 4 blocks of 256 threads per SM (64 registers, no
+// spill: the atmosphere segment is formed after the layer chain); the
+// height-average mode and FP64 keep 3 (more live values).
 template <bool MIXED, int TE, int MODE>
-__global__ void __launch_bounds__(MIXED ? 256 : 128, 3) propagate_kernel(PropArgs a) {
+__global__ void __launch_bounds__(MIXED ? 256 : 128, (MIXED && MODE != kModeHeights) ? 4 : 3)
+    propagate_kernel(PropArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const TileSmem L = tile_smem(MIXED, TE, a.nl, a.nl_pad, a.cchunk);
     stage_phase_table<MIXED>(smem, L, a.ptab);
