@@ -18,9 +18,9 @@
 //                     matrix from the tables (no per-layer storage: the chain is
 //                     un-multiplied with T^T and conj(D)); per-(energy, layer)
 //                     adjoints are summed over the warp's cosines with shuffles
-//   ll_layer_kernel   one block per energy, one thread per layer: sums the
-//                     warps' partials, re-solves the layer's eigen-problem in
-//                     FP64 and back-propagates through it to the parameters
+//   ll_layer_kernel   one block per energy, three threads (rows) per layer:
+//                     sums the warps' partials and back-propagates through the
+//                     layer's FP64 eigen-decomposition to the parameters
 //   ll_sum_kernel     sums the per-energy rows (fixed order: deterministic)
 // Precision: FP64 does every step in double; MIXED runs ll_pair_kernel in
 // FP32 (phases in double-float) with the FP64 tables and FP64 reduction.
@@ -577,229 +577,202 @@ __global__ void __launch_bounds__(128) ll_pair_kernel(LLArgs a) {
 // theta23, dCP, dm12sq, dm23sq, [7 + r] density of the caller's row r.
 constexpr int kLLOscOut = 7;
 
-// Lanes per energy in ll_layer_kernel: 8 or 16 when the layers fit (2 or 4
-// energies share a warp), else a multiple of 32.
-__host__ __device__ inline int ll_layer_lanes(int nl) { return nl <= 8 ? 8 : nl <= 16 ? 16 : (nl + 31) / 32 * 32; }
+// Lanes per row group of ll_layer_kernel: the layers rounded up to a warp.
+__host__ __device__ inline int ll_layer_lanes(int nl) { return (nl + 31) / 32 * 32; }
 
-// Energy slot s of block b is energy b * EPB + s (EPB = blockDim.x / S, S =
-// ll_layer_lanes); its thread l < nl handles layer l.  The thread sums the
-// warps' partials of its layer, takes the layer's FP64 eigen-pairs from the
-// prep kernel, the adjoint of its eigenvectors from the two overlaps it
-// enters (T_{l-1} = V_l^T V_{l-1} and T_l = V_{l+1}^T V_l, neighbours through
-// shared memory) and back-propagates through the eigen-decomposition to the
-// parameters.  The rows of the body map one-to-one to layers 1..nl-1, so each
-// density slot has a single writer; the oscillation parameters are summed
-// over the energy's lanes in a fixed order.
-__global__ void __launch_bounds__(96) ll_layer_kernel(LLArgs a) {
+// Block e: energy e.  Thread (r, l) = (threadIdx.x / S, threadIdx.x % S),
+// S = ll_layer_lanes(nl), handles row r in {0, 1, 2} of the 3x3 quantities of
+// layer l < nl, so that the FP64 chain of each (energy, layer) is split
+// three ways (the work is 2 x 10^3 short chains: latency, not throughput):
+//   1. sums of the warps' partials (11 per layer) and the eigen-pairs solved by
+//      the prep kernel, into shared memory;
+//   2. row r of the eigenvector adjoint gV_l from the two overlaps the layer
+//      enters (T_{l-1} = V_l^T V_{l-1}, T_l = V_{l+1}^T V_l) and, for l = 0, 1,
+//      from Gamma' / Lambda';
+//   3. row r of W, W[j][k] = (v_j . gv_k) / (m_k - m_j) off the diagonal and
+//      dLL/dm_k on it (symmetric eigenvector adjoint);
+//   4. row r of gH = V W V^T;
+//   5. row r's share of the contractions of sym(gH) with the parameter
+//      derivatives of H_l = O diag(0, d1, d2) O^T - fac_l e0 e0^T.
+// Densities map one-to-one to layers (single writer per slot); the
+// oscillation parameters are summed over the block in a fixed order.
+__global__ void __launch_bounds__(288) ll_layer_kernel(LLArgs a) {
     extern __shared__ double s_ll[];
-    const int nl = a.nl, S = ll_layer_lanes(nl), EPB = max(1, (int)blockDim.x / S);
-    const int slot = threadIdx.x / S, l = threadIdx.x % S;
-    const int e = blockIdx.x * EPB + slot;
-    const bool live_e = e < a.n_en;
-    double* sV = s_ll + (size_t)slot * nl * 9;                   // [EPB][nl][9]
-    double* sT = s_ll + (size_t)EPB * nl * 9 + (size_t)slot * nl * 9;
-    double* sL = s_ll + (size_t)2 * EPB * nl * 9 + (size_t)slot * kLLPerE;
-    double* sRed = s_ll + (size_t)2 * EPB * nl * 9 + (size_t)EPB * kLLPerE;  // [blockDim/32][7]
+    const int nl = a.nl, S = ll_layer_lanes(nl);
+    const int r = threadIdx.x / S, l = threadIdx.x % S;
+    const int e = blockIdx.x;
+    double* sV = s_ll;                 // [nl][9]
+    double* sT = sV + nl * 9;          // [nl][9] summed adjoint of T_l
+    double* sK = sT + nl * 9;          // [nl][2] summed adjoint of kappa_l
+    double* sM = sK + nl * 2;          // [nl][3] eigenvalues
+    double* sG = sM + nl * 3;          // [nl][9] gV, then W, then gH
+    double* sL = sG + nl * 9;          // [19]
+    double* sRed = sL + kLLPerE;       // [blockDim / 32][7]
     const OscParams& o = *a.osc;
-    const double E = live_e ? a.energies[e] : 1.0;
-    double gT[9], gK0 = 0.0, gK1 = 0.0, m[3], V[9];
-#pragma unroll
-    for (int q = 0; q < 9; q++) gT[q] = 0.0;
-    const bool live = live_e && l < nl;
+    const double E = a.energies[e];
+    const bool live = l < nl;
+    // 1. partial sums (float from the mixed pair kernel), eigen-pairs
     if (live) {
-        // the warps' partials (float from the mixed pair kernel), summed in FP64
-        if (a.part_l_f) {
-            for (int cc = 0; cc < a.n_cchunk; cc++) {
-                const float* pl = a.part_l_f + (((size_t)cc * a.n_en + e) * nl + l) * kLLPerL;
-#pragma unroll
-                for (int q = 0; q < 9; q++) gT[q] += (double)pl[q];
-                gK0 += (double)pl[9];
-                gK1 += (double)pl[10];
-            }
-        } else {
-            for (int cc = 0; cc < a.n_cchunk; cc++) {
-                const double* pl = a.part_l + (((size_t)cc * a.n_en + e) * nl + l) * kLLPerL;
-#pragma unroll
-                for (int q = 0; q < 9; q++) gT[q] += pl[q];
-                gK0 += pl[9];
-                gK1 += pl[10];
-            }
-        }
-        // eigen-pairs of this (energy, layer) as solved by the prep kernel
-        const double* ev = a.eig + ((size_t)e * nl + l) * kLLEigWords;
-#pragma unroll
-        for (int q = 0; q < 9; q++) V[q] = ev[q];
-#pragma unroll
-        for (int k = 0; k < 3; k++) m[k] = ev[9 + k];
-#pragma unroll
-        for (int q = 0; q < 9; q++) {
-            sV[l * 9 + q] = V[q];
-            sT[l * 9 + q] = gT[q];
-        }
-    }
-    if (live_e)
-        for (int w = l; w < kLLPerE; w += S) {
+        for (int q = r; q < kLLPerL; q += 3) {
             double v = 0.0;
             for (int cc = 0; cc < a.n_cchunk; cc++) {
-                const size_t i = ((size_t)cc * a.n_en + e) * kLLPerE + w;
-                v += a.part_e_f ? (double)a.part_e_f[i] : a.part_e[i];
+                const size_t i = (((size_t)cc * a.n_en + e) * nl + l) * kLLPerL + q;
+                v += a.part_l_f ? (double)a.part_l_f[i] : a.part_l[i];
             }
-            sL[w] = v;
+            if (q < 9)
+                sT[l * 9 + q] = v;
+            else
+                sK[l * 2 + q - 9] = v;
         }
+        const double* ev = a.eig + ((size_t)e * nl + l) * kLLEigWords;
+#pragma unroll
+        for (int k = 0; k < 3; k++) sV[l * 9 + 3 * r + k] = ev[3 * r + k];
+        sM[l * 3 + r] = ev[9 + r];
+    }
+    for (int w = threadIdx.x; w < kLLPerE; w += blockDim.x) {
+        double v = 0.0;
+        for (int cc = 0; cc < a.n_cchunk; cc++) {
+            const size_t i = ((size_t)cc * a.n_en + e) * kLLPerE + w;
+            v += a.part_e_f ? (double)a.part_e_f[i] : a.part_e[i];
+        }
+        sL[w] = v;
+    }
     __syncthreads();
 
     double acc[kLLOscOut];
 #pragma unroll
     for (int q = 0; q < kLLOscOut; q++) acc[q] = 0.0;
-    const int np = 6 + a.n_rows;
-    double* grow = a.part_g + (size_t)(live_e ? e : 0) * (1 + np);
+    const double s23 = o.s23, c23 = o.c23, sd = o.sd, cd = o.cd;
+    // 2. row r of gV_l
+    double gvr[3] = {0.0, 0.0, 0.0};
     if (live) {
-        const double s23 = o.s23, c23 = o.c23, sd = o.sd, cd = o.cd;
-        double gV[9];
+        // T_l = V_{l+1}^T V_l: dT_l[i][c] / dV_l[r][c] = V_{l+1}[r][i]
+        if (l + 1 < nl)
 #pragma unroll
-        for (int q = 0; q < 9; q++) gV[q] = 0.0;
-        // T_l = V_{l+1}^T V_l: dT_l[i][j] / dV_l[r][j] = V_{l+1}[r][i]
-        if (l + 1 < nl) {
+            for (int c = 0; c < 3; c++)
 #pragma unroll
-            for (int i = 0; i < 3; i++)
+                for (int i = 0; i < 3; i++) gvr[c] += sT[l * 9 + 3 * i + c] * sV[(l + 1) * 9 + 3 * r + i];
+        // T_{l-1} = V_l^T V_{l-1}: dT_{l-1}[c][j] / dV_l[r][c] = V_{l-1}[r][j]
+        if (l >= 1)
 #pragma unroll
-                for (int j = 0; j < 3; j++)
+            for (int c = 0; c < 3; c++)
 #pragma unroll
-                    for (int r = 0; r < 3; r++) gV[3 * r + j] += sT[l * 9 + 3 * i + j] * sV[(l + 1) * 9 + 3 * r + i];
-        }
-        // T_{l-1} = V_l^T V_{l-1}: dT_{l-1}[i][j] / dV_l[r][i] = V_{l-1}[r][j]
-        if (l >= 1) {
+                for (int j = 0; j < 3; j++) gvr[c] += sT[(l - 1) * 9 + 3 * c + j] * sV[(l - 1) * 9 + 3 * r + j];
+        if (l <= 1) {
+            // l = 1, Lambda' from V_1: row 0 = V_1[0][k]; row 1 = c23 V_1[1][k] + s23 e^{i d} V_1[2][k]
+            // l = 0, Gamma' from V_0: column 0 = V_0[0][k]; column 1 = c23 V_0[1][k] + s23 e^{-i d} V_0[2][k]
+            const int off = (l == 1) ? 0 : 9;
+            const double sg = (l == 1) ? 1.0 : -1.0;
 #pragma unroll
-            for (int i = 0; i < 3; i++)
-#pragma unroll
-                for (int j = 0; j < 3; j++)
-#pragma unroll
-                    for (int r = 0; r < 3; r++)
-                        gV[3 * r + i] += sT[(l - 1) * 9 + 3 * i + j] * sV[(l - 1) * 9 + 3 * r + j];
-        }
-        if (l == 1) {
-            // Lambda' from V_1: row 0 = V_1[0][k]; row 1 = c23 V_1[1][k] + s23 e^{i d} V_1[2][k]
             for (int k = 0; k < 3; k++) {
-                const double gre = sL[3 + 2 * k], gim = sL[4 + 2 * k];
-                gV[k] += sL[k];
-                gV[3 + k] += c23 * gre;
-                gV[6 + k] += s23 * (gre * cd + gim * sd);
-                const double v1 = V[3 + k], v2 = V[6 + k];
-                // d/dtheta23: -s23 v1 + c23 e^{id} v2 ; d/ddcp: i s23 e^{id} v2
-                acc[3] += gre * (-s23 * v1 + c23 * cd * v2) + gim * (c23 * sd * v2);
-                acc[4] += gre * (-s23 * sd * v2) + gim * (s23 * cd * v2);
+                const double gre = sL[off + 3 + 2 * k], gim = sL[off + 4 + 2 * k];
+                if (r == 0) gvr[k] += sL[off + k];
+                if (r == 1) gvr[k] += c23 * gre;
+                if (r == 2) gvr[k] += s23 * (gre * cd + sg * gim * sd);
+                if (r == 0) {
+                    const double v1 = sV[l * 9 + 3 + k], v2 = sV[l * 9 + 6 + k];
+                    // d/dtheta23: -s23 v1 + c23 e^{+-id} v2 ; d/ddcp: +-i s23 e^{+-id} v2
+                    acc[3] += gre * (-s23 * v1 + c23 * cd * v2) + gim * (sg * c23 * sd * v2);
+                    acc[4] += gre * (-s23 * sd * v2) + gim * (sg * s23 * cd * v2);
+                }
+            }
+            if (l == 0 && r == 0) acc[0] = sL[18];
+        }
+    }
+    __syncthreads();  // sG free (never read before): write gV
+    if (live)
+#pragma unroll
+        for (int c = 0; c < 3; c++) sG[l * 9 + 3 * r + c] = gvr[c];
+    __syncthreads();
+    // 3. row j = r of W
+    double wr[3];
+    if (live) {
+        const double f = phase_rate_factor(E);
+        const double gK0 = sK[l * 2], gK1 = sK[l * 2 + 1];
+        const double gm[3] = {-(gK0 + gK1) * f, gK0 * f, gK1 * f};
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            if (k == r) {
+                wr[k] = gm[k];
+            } else {
+                double dot = 0.0;
+#pragma unroll
+                for (int q = 0; q < 3; q++) dot += sV[l * 9 + 3 * q + r] * sG[l * 9 + 3 * q + k];
+                const double gap = sM[l * 3 + k] - sM[l * 3 + r];
+                wr[k] = (gap != 0.0) ? dot / gap : 0.0;
             }
         }
-        if (l == 0) {
-            // Gamma' from V_0: column 0 = V_0[0][k]; column 1 = c23 V_0[1][k] + s23 e^{-i d} V_0[2][k]
-            for (int k = 0; k < 3; k++) {
-                const double gre = sL[12 + 2 * k], gim = sL[13 + 2 * k];
-                gV[k] += sL[9 + k];
-                gV[3 + k] += c23 * gre;
-                gV[6 + k] += s23 * (gre * cd - gim * sd);
-                const double v1 = V[3 + k], v2 = V[6 + k];
-                acc[3] += gre * (-s23 * v1 + c23 * cd * v2) + gim * (-c23 * sd * v2);
-                acc[4] += gre * (-s23 * sd * v2) + gim * (-s23 * cd * v2);
-            }
-            acc[0] = sL[18];
-        }
-        // eigen back-propagation; H_l = O diag(0, d1, d2) O^T - fac_l e0 e0^T.
-        // O = R13 R12 and its derivatives from the stored O matrix.
+    }
+    __syncthreads();
+    if (live)
+#pragma unroll
+        for (int k = 0; k < 3; k++) sG[l * 9 + 3 * r + k] = wr[k];
+    __syncthreads();
+    // 4. row p = r of gH = V W V^T: u_k = sum_j V[r][j] W[j][k], gH[r][q] = sum_k u_k V[q][k]
+    double hr[3] = {0.0, 0.0, 0.0};
+    if (live) {
+        double u[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) u[k] += sV[l * 9 + 3 * r + j] * sG[l * 9 + 3 * j + k];
+#pragma unroll
+        for (int q = 0; q < 3; q++)
+#pragma unroll
+            for (int k = 0; k < 3; k++) hr[q] += u[k] * sV[l * 9 + 3 * q + k];
+    }
+    __syncthreads();
+    if (live)
+#pragma unroll
+        for (int q = 0; q < 3; q++) sG[l * 9 + 3 * r + q] = hr[q];
+    __syncthreads();
+    // 5. contractions of row r of sym(gH)
+    if (live) {
         const double* O = o.o;
         const double c13 = O[8], s13 = O[2];
         const double c12 = (c13 != 0.0) ? O[0] / c13 : O[4];
         const double sn12 = -O[3];
         const double dO12[9] = {-c13 * sn12, c13 * c12, 0.0, -c12, -sn12, 0.0, s13 * sn12, -s13 * c12, 0.0};
         const double dO13[9] = {-s13 * c12, -s13 * sn12, c13, 0.0, 0.0, 0.0, -c13 * c12, -c13 * sn12, -s13};
-        // dLL/dm_k from the phase rates kappa_k = -LoE (m_k - m_0) / (2 pi E), k = 1, 2
-        const double f = phase_rate_factor(E);
-        const double gm[3] = {-(gK0 + gK1) * f, gK0 * f, gK1 * f};
-        // gH = sum_k gm_k v_k v_k^T + sum_{k != j} (v_j . gv_k) / (m_k - m_j) v_j v_k^T
-        double W[3][3];  // W[j][k] = coefficient of v_j v_k^T
-#pragma unroll
-        for (int j = 0; j < 3; j++)
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                if (j == k) {
-                    W[j][k] = gm[k];
-                } else {
-                    double dot = 0.0;
-#pragma unroll
-                    for (int r = 0; r < 3; r++) dot += V[3 * r + j] * gV[3 * r + k];
-                    const double gap = m[k] - m[j];
-                    W[j][k] = (gap != 0.0) ? dot / gap : 0.0;
-                }
-            }
-        double gH[3][3];
-#pragma unroll
-        for (int p = 0; p < 3; p++)
-#pragma unroll
-            for (int q = 0; q < 3; q++) {
-                double sum = 0.0;
-#pragma unroll
-                for (int j = 0; j < 3; j++)
-#pragma unroll
-                    for (int k = 0; k < 3; k++) sum += W[j][k] * V[3 * p + j] * V[3 * q + k];
-                gH[p][q] = sum;
-            }
-#pragma unroll
-        for (int p = 0; p < 3; p++)
-#pragma unroll
-            for (int q = p + 1; q < 3; q++) {
-                const double sym = 0.5 * (gH[p][q] + gH[q][p]);
-                gH[p][q] = gH[q][p] = sym;
-            }
-        double gd1 = 0.0, gd2 = 0.0, gth12 = 0.0, gth13 = 0.0;
         const double dd[3] = {0.0, o.d1, o.d2};
+        double gd1 = 0.0, gd2 = 0.0, gth12 = 0.0, gth13 = 0.0;
 #pragma unroll
-        for (int p = 0; p < 3; p++)
+        for (int q = 0; q < 3; q++) {
+            const double h = 0.5 * (sG[l * 9 + 3 * r + q] + sG[l * 9 + 3 * q + r]);
+            // d1, d2: o_1^T gH o_1, o_2^T gH o_2
+            gd1 += h * O[3 * r + 1] * O[3 * q + 1];
+            gd2 += h * O[3 * r + 2] * O[3 * q + 2];
+            // theta12, theta13: 2 tr(gH O D dO^T)
 #pragma unroll
-            for (int q = 0; q < 3; q++) {
-                // d1, d2: o_1^T gH o_1, o_2^T gH o_2
-                gd1 += gH[p][q] * O[3 * p + 1] * O[3 * q + 1];
-                gd2 += gH[p][q] * O[3 * p + 2] * O[3 * q + 2];
-                // theta12, theta13: 2 tr(gH O D dO^T)
-#pragma unroll
-                for (int k = 1; k < 3; k++) {
-                    gth12 += 2.0 * gH[p][q] * O[3 * p + k] * dd[k] * dO12[3 * q + k];
-                    gth13 += 2.0 * gH[p][q] * O[3 * p + k] * dd[k] * dO13[3 * q + k];
-                }
+            for (int k = 1; k < 3; k++) {
+                gth12 += 2.0 * h * O[3 * r + k] * dd[k] * dO12[3 * q + k];
+                gth13 += 2.0 * h * O[3 * r + k] * dd[k] * dO13[3 * q + k];
             }
+        }
         acc[1] = gth12;
         acc[2] = gth13;
         // d1 = dm12sq, d2 = dm12sq + dm23sq
         acc[5] = gd1 + gd2;
         acc[6] = gd2;
         // densities: H[0][0] -= fac, fac = sgn GF E rho Ye
-        if (l >= 1) {
+        if (l >= 1 && r == 0) {
             const double sgn = a.anti ? 1.0 : -1.0;
-            grow[1 + 6 + a.layer_row[l]] = -gH[0][0] * sgn * kGF * E * a.ye_layer[l];
+            const int np = 6 + a.n_rows;
+            a.part_g[(size_t)e * (1 + np) + 1 + 6 + a.layer_row[l]] = -sG[l * 9] * sgn * kGF * E * a.ye_layer[l];
         }
     }
-    // fixed-order sum of the oscillation slots over the energy's lanes:
-    // butterflies inside S-lane segments (S <= 32), then across warps
+    // fixed-order sum over the block: warp butterflies, then the warps in order
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int width = S < 32 ? S : 32;
 #pragma unroll
     for (int q = 0; q < kLLOscOut; q++) {
-        double v = acc[q];
-        for (int off = width >> 1; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-        acc[q] = v;
+        const double v = warp_sum(acc[q]);
+        if (lane == 0) sRed[w * kLLOscOut + q] = v;
     }
-    if (S <= 32) {
-        if (l == 0 && live_e)
-#pragma unroll
-            for (int q = 0; q < kLLOscOut; q++) grow[q] = acc[q];
-    } else {
-        if (lane == 0)
-#pragma unroll
-            for (int q = 0; q < kLLOscOut; q++) sRed[w * kLLOscOut + q] = acc[q];
-        __syncthreads();
-        if ((int)threadIdx.x < kLLOscOut && live_e) {
-            double v = 0.0;
-            for (int i = 0; i < (int)(blockDim.x >> 5); i++) v += sRed[i * kLLOscOut + threadIdx.x];
-            grow[threadIdx.x] = v;
-        }
+    __syncthreads();
+    if ((int)threadIdx.x < kLLOscOut) {
+        double v = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) v += sRed[i * kLLOscOut + threadIdx.x];
+        a.part_g[(size_t)e * (7 + a.n_rows) + threadIdx.x] = v;
     }
 }
 
@@ -1023,9 +996,9 @@ int ll_setup(cp3_loglik* L, int type) {
         e = cudaGetLastError();
     }
     if (!e) {
-        const int S = cp3::ll_layer_lanes(L->nl), epb = std::max(1, 32 / S), threads = epb * S;
-        const size_t smem = ((size_t)2 * epb * L->nl * 9 + (size_t)epb * cp3::kLLPerE + (size_t)(threads / 32) * 7) * 8;
-        cp3::ll_layer_kernel<<<(L->n_en + epb - 1) / epb, threads, smem, cs>>>(a);
+        const int threads = 3 * cp3::ll_layer_lanes(L->nl);
+        const size_t smem = ((size_t)L->nl * (9 + 9 + 2 + 3 + 9) + cp3::kLLPerE + (size_t)(threads / 32) * 7) * 8;
+        cp3::ll_layer_kernel<<<L->n_en, threads, smem, cs>>>(a);
         e = cudaGetLastError();
     }
     if (!e) {
