@@ -372,10 +372,25 @@ def run_ours(args, world, rank, local):
     if not args.skip_fp64:
         fprops, fbufs = build("fp64")
         fsteps = max(1, min(args.steps, 3))
-        ftimes = timed_steps(fprops, fsteps, 1)
+        for p, _ in fprops:
+            p.set_kernel_timing(True)
+        fkt = []
+        ftimes = timed_steps(fprops, fsteps, 1, fkt)
+        for p, _ in fprops:
+            p.set_kernel_timing(False)
         fms = allmax(world, sum(ftimes) / len(ftimes))
+        fprop_ms = float(np.mean([k[1] for k in fkt]))
+        # the same chain in FP64: one DFMA per multiply-add of the mixed
+        # kernel's count, against the live-measured DFMA peak of this GPU
         fp64 = {"value": world * pairs_step / (fms * 1e-3), "unit": "pairs/s", "ms_per_step": fms,
-                "steps": fsteps}
+                "steps": fsteps,
+                "roofline": {"bound": "fp64 pipe (DFMA)", "kernel": "propagate_kernel<fp64>",
+                             "kernel_ms": fprop_ms, "work_per_launch": madw,
+                             "achieved": madw / (fprop_ms * 1e-3) / 1e12, "peak": peak_dfma / 1e12,
+                             "unit": "T DFMA/s", "frac": (madw / (fprop_ms * 1e-3)) / peak_dfma,
+                             "note": "chain multiply-adds only; the FP64 phases (sincospi) and the "
+                                     "completion come on top",
+                             "peak_source": "measured live on this GPU (cp3_pipe_peak)"}}
         # precision of this step's mixed results against FP64 (every pair)
         for p, t in props:
             p.calculateProbabilitiesAsync(t)
@@ -485,13 +500,16 @@ def run_batch(args, world, rank, local):
     b.calculate(0)
     flat = b.results()
     err = 0.0
+    errs = []
     for s_ in range(0, n, max(1, n // 8)):
         got = b.set_result(flat, s_)
         ic = np.arange(0, nc[s_], 16)
         ie = np.arange(0, ne[s_], 16)
         want = oracle.calculate(cos[s_][ic], en[s_][ie], B.radii, B.rho_eff() * scale[s_], tuple(params[s_]),
                                 22.0, False)
-        err = max(err, float(np.abs(got[:, ic][:, :, ie].astype(np.float64) - want).max()))
+        d = np.abs(got[:, ic][:, :, ie].astype(np.float64) - want)
+        err = max(err, float(d.max()))
+        errs.append(float(d.mean()))
     te, groups, cchunk, blocks = b.launch_shape()
     if rank == 0:
         line = {"metric": "(cos,E) pairs/s, %d parameter sets with uneven grids in one persistent CUDA-graph "
@@ -509,7 +527,9 @@ def run_batch(args, world, rank, local):
                 "sequential": {"value": world * pairs / (seq_ms * 1e-3), "unit": "pairs/s", "ms_per_step": seq_ms,
                                "launches_per_step": 2 * n},
                 "speedup_vs_sequential": seq_ms / ms, "gpu_launches": 1 + 2 * args.steps,
-                "precision": {"max_abs_dp_vs_oracle_sampled_sets": err}}
+                "precision": {"max_abs_dp_vs_oracle_sampled_sets": err,
+                              "mean_abs_dp_vs_oracle_sampled_sets": float(np.mean(errs)),
+                              "sampled": "every %d-th set, every 16th cosine and energy" % max(1, n // 8)}}
         print(json.dumps(line), flush=True)
     b.close()
 
@@ -676,6 +696,7 @@ def run_heights(args, world, rank, local):
     # parity on a strided subset: every 64th cosine and energy
     idx = np.arange(0, NC, 64)
     err = 0.0
+    means = []
     for (p, t), buf in zip(props, bufs):
         p.calculateProbabilities(t)
         got = buf.cpu().numpy()[:, idx][:, :, idx].astype(np.float64)
@@ -683,6 +704,7 @@ def run_heights(args, world, rank, local):
         want = sum(wk * oracle.calculate(cos[idx], en[idx], B.radii, B.rho_eff(), nom, float(h),
                                          t == cp.Antineutrino) for h, wk in zip(heights, w))
         err = max(err, float(np.abs(got - want).max()))
+        means.append(float(np.abs(got - want).mean()))
     pairs_step = 2 * NC * NE
     if rank == 0:
         line = {"metric": "(cos,E) pairs/s with probabilities averaged over 8 production heights (mixed)",
@@ -698,6 +720,7 @@ def run_heights(args, world, rank, local):
                 "cost_vs_single_height": ms / single_ms,
                 "gpu_launches": 2 * 2 * args.steps, "clocks": clocks,
                 "precision": {"max_abs_dp_vs_oracle_height_average_subset": err,
+                              "mean_abs_dp_vs_oracle_height_average_subset": float(np.mean(means)),
                               "subset": "every 64th cosine x every 64th energy, nu and nubar"}}
         print(json.dumps(line), flush=True)
     for p, _ in props:
