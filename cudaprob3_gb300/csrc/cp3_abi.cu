@@ -206,19 +206,10 @@ int cp3_create(cp3_propagator** out, int device_id, int n_cosines, int n_energie
     if ((e = p->d_maxl.ensure(std::max(n_cosines, 1))) != cudaSuccess) return bail(e, "cudaMalloc");
     if ((e = p->d_result.ensure(std::max<size_t>(p->result_bytes(), 16))) != cudaSuccess)
         return bail(e, "cudaMalloc");
-    if (p->mixed) {
-        // cos/sin of 2*pi*j/256, j = -128..128, in Q1.30 and as float
+    {
+        // cos/sin of 2*pi*j/256, j = -128..128 (Q1.30 and float, or FP64)
         std::vector<int4> tab(cp3::kPhaseTabN + 1);
-        for (int j = -cp3::kPhaseTabN / 2; j <= cp3::kPhaseTabN / 2; j++) {
-            const double ang = cp3::kTwoPi * j / cp3::kPhaseTabN;
-            const double c = std::cos(ang), s = std::sin(ang);
-            float cf = (float)c, sf = (float)s;
-            int ci, si;
-            std::memcpy(&ci, &cf, 4);
-            std::memcpy(&si, &sf, 4);
-            tab[j + cp3::kPhaseTabN / 2] =
-                make_int4((int)std::llround(c * 1073741824.0), (int)std::llround(s * 1073741824.0), ci, si);
-        }
+        cp3::fill_phase_table(p->mixed, tab.data());
         if ((e = p->d_ptab.ensure(tab.size())) != cudaSuccess) return bail(e, "cudaMalloc");
         if ((e = cudaMemcpy(p->d_ptab.p, tab.data(), tab.size() * sizeof(int4), cudaMemcpyHostToDevice)) !=
             cudaSuccess)

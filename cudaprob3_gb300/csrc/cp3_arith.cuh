@@ -274,11 +274,34 @@ struct F64 {
     }
 };
 
+// FP64 cos/sin of 2 pi u for |u| <= 1/2, from the 257-entry table tab[j + 128]
+// = (cos, sin)(2 pi j / 256): u = j / 256 + d with j = rint(256 u) (d exact,
+// |d| <= 1/512), x = 2 pi d, the Taylor series of sin x to x^7 and of
+// cos x - 1 to x^8 (truncation below 2e-23 for |x| <= pi/256), rotated onto
+// the table entry.  About 1 ulp; a third of the FP64 work of a general sincos.
+__device__ __forceinline__ void sincos_turns_f64(double u, const double2* __restrict__ tab, double& c,
+                                                 double& s) {
+    double j = rint(u * 256.0);
+    j = fmin(fmax(j, -128.0), 128.0);
+    const double d = fma(j, -0.00390625, u);
+    const double x = d * kTwoPi;
+    const double x2 = x * x;
+    double p = fma(x2, -1.0 / 5040.0, 1.0 / 120.0);
+    p = fma(x2, p, -1.0 / 6.0);
+    const double sx = fma(x * x2, p, x);  // sin x
+    double q = fma(x2, 1.0 / 40320.0, -1.0 / 720.0);
+    q = fma(x2, q, 1.0 / 24.0);
+    q = fma(x2, q, -0.5);
+    const double cm1 = x2 * q;  // cos x - 1
+    const double2 e = tab[(int)j + 128];
+    c = e.x + fma(-e.y, sx, e.x * cm1);
+    s = e.y + fma(e.x, sx, e.y * cm1);
+}
+
 // FP64 cos/sin of 2*pi*t, t = kappa * L turns.
-__device__ __forceinline__ void phase_f64(double kappa, double L, double& c, double& s) {
+__device__ __forceinline__ void phase_f64(double kappa, double L, const double2* tab, double& c, double& s) {
     const double t = kappa * L;
-    const double r = t - rint(t);
-    sincospi(2.0 * r, &s, &c);
+    sincos_turns_f64(t - rint(t), tab, c, s);
 }
 
 }  // namespace cp3

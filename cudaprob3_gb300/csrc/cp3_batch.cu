@@ -645,16 +645,7 @@ int cp3_batch_create(cp3_batch** out, int device_id, int precision, int n_sets, 
     if ((e = b->d_counter.ensure(1))) return bail(e, "cudaMalloc");
     if ((e = cudaEventCreate(&b->ev[0])) || (e = cudaEventCreate(&b->ev[1]))) return bail(e, "cudaEventCreate");
     std::vector<int4> tab(cp3::kPhaseTabN + 1);
-    for (int j = -cp3::kPhaseTabN / 2; j <= cp3::kPhaseTabN / 2; j++) {
-        const double ang = cp3::kTwoPi * j / cp3::kPhaseTabN;
-        const double c = std::cos(ang), s = std::sin(ang);
-        float cf = (float)c, sf = (float)s;
-        int ci, si;
-        std::memcpy(&ci, &cf, 4);
-        std::memcpy(&si, &sf, 4);
-        tab[j + cp3::kPhaseTabN / 2] =
-            make_int4((int)std::llround(c * 1073741824.0), (int)std::llround(s * 1073741824.0), ci, si);
-    }
+    cp3::fill_phase_table(b->mixed, tab.data());
     if ((e = b->d_ptab.ensure(tab.size())) ||
         (e = cudaMemcpy(b->d_ptab.p, tab.data(), tab.size() * sizeof(int4), cudaMemcpyHostToDevice)))
         return bail(e, "phase table");

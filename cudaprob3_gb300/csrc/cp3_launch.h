@@ -3,7 +3,9 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstddef>
+#include <cstring>
 #include <string>
 
 #include "cp3_internal.h"
@@ -55,6 +57,27 @@ cudaError_t launch_prep(bool mixed, PrepArgs a, cudaStream_t s);
 // mode: 0 planes, 1 fused rates, 2 planes averaged over production heights
 cudaError_t launch_propagate(bool mixed, const PropArgs& a, int te, int groups, size_t smem,
                              cudaStream_t s, int mode = 0);
+
+// The 257-entry phase table of the propagate kernels, j = -128..128 at index
+// j + 128: mixed (Q1.30 cos, Q1.30 sin, float cos, float sin) of 2*pi*j/256;
+// FP64 (double cos, double sin) in the same 16 bytes.
+inline void fill_phase_table(bool mixed, int4* tab) {
+    for (int j = -kPhaseTabN / 2; j <= kPhaseTabN / 2; j++) {
+        const double ang = kTwoPi * j / kPhaseTabN;
+        const double c = std::cos(ang), s = std::sin(ang);
+        int4& out = tab[j + kPhaseTabN / 2];
+        if (mixed) {
+            const float cf = (float)c, sf = (float)s;
+            int ci, si;
+            std::memcpy(&ci, &cf, 4);
+            std::memcpy(&si, &sf, 4);
+            out = make_int4((int)std::llround(c * 1073741824.0), (int)std::llround(s * 1073741824.0), ci, si);
+        } else {
+            const double cs[2] = {c, s};
+            std::memcpy(&out, cs, sizeof cs);
+        }
+    }
+}
 
 // Message returned by cp3_last_error() on this thread.
 void set_last_error(const std::string& msg);

@@ -55,15 +55,18 @@ struct NoAllocBody {
 // Writes the layer radii and densities, the Q1.30/float cos-sin table and the
 // layer count of every cosine (propagator.hpp:301-307) into the scratch.
 __global__ void noalloc_setup_kernel(NoAllocBody body, const double* cosines, int n_cos, double* radii,
-                                     double* rhoye, int4* ptab, int* maxl) {
+                                     double* rhoye, int4* ptab, int* maxl, int mixed) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < body.n) radii[t] = body.radii[t];
     if (t <= body.n) rhoye[t] = body.rhoye[t];
     if (t <= kPhaseTabN) {
         double s, c;
         sincospi((double)(t - kPhaseTabN / 2) / (kPhaseTabN / 2), &s, &c);
-        ptab[t] = make_int4((int)__double2ll_rn(c * 1073741824.0), (int)__double2ll_rn(s * 1073741824.0),
-                            __float_as_int(__double2float_rn(c)), __float_as_int(__double2float_rn(s)));
+        if (mixed)
+            ptab[t] = make_int4((int)__double2ll_rn(c * 1073741824.0), (int)__double2ll_rn(s * 1073741824.0),
+                                __float_as_int(__double2float_rn(c)), __float_as_int(__double2float_rn(s)));
+        else
+            ((double2*)ptab)[t] = make_double2(c, s);
     }
     if (t < n_cos) {
         const double cz = cosines[t];
@@ -170,7 +173,7 @@ extern "C" int cp3_propagate_noalloc(int precision, int type, const double* d_co
     {
         const int n = std::max(n_cosines, kPhaseTabN + 1);
         noalloc_setup_kernel<<<(n + 255) / 256, 256, 0, s>>>(body, d_cosines, n_cosines, d_radii, d_rhoye, ptab,
-                                                             maxl);
+                                                             maxl, precision == CP3_PRECISION_MIXED ? 1 : 0);
         if ((e = cudaGetLastError()) != cudaSuccess)
             return nfail(CP3_ERR_CUDA, std::string("setup kernel: ") + cudaGetErrorString(e));
     }

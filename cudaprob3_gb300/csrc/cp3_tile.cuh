@@ -162,6 +162,7 @@ struct F64Src {
     const double* tab;  // shared: [nl][11][TE], offset by lane
     const double* pe;
     const double* len;
+    const double2* ptab;  // shared: 257 (cos, sin) of 2*pi*j/256
     __device__ __forceinline__ double T(int l, int i, int j) const { return tab[(l * kFp64Words + 3 * i + j) * TE]; }
     __device__ __forceinline__ double La(int j) const { return pe[j * TE]; }
     __device__ __forceinline__ F64::C Lb(int j) const { return F64::C{pe[(3 + 2 * j) * TE], pe[(4 + 2 * j) * TE]}; }
@@ -174,8 +175,8 @@ struct F64Src {
     __device__ __forceinline__ void phase_len(int l, double L, double& c1, double& s1, double& n1, double& c2,
                                               double& s2, double& n2) const {
         const double* k = tab + (l * kFp64Words + 9) * TE;
-        phase_f64(k[0], L, c1, s1);
-        phase_f64(k[TE], L, c2, s2);
+        phase_f64(k[0], L, ptab, c1, s1);
+        phase_f64(k[TE], L, ptab, c2, s2);
         n1 = -s1;
         n2 = -s2;
     }
@@ -192,7 +193,7 @@ struct F64Src {
         acc.t -= rint(acc.t);
     }
     __device__ __forceinline__ void turns_phase(const Turns& acc, double& c, double& s) const {
-        sincospi(2.0 * acc.t, &s, &c);
+        sincos_turns_f64(acc.t, ptab, c, s);
     }
 };
 
@@ -216,7 +217,7 @@ __host__ __device__ inline TileSmem tile_smem(bool mixed, int te, int nl, int nl
     t.tab = 0;
     t.pe = t.tab + (size_t)nl * W * te * word;
     t.ptab = t.pe + (size_t)kPerEWords * te * word;
-    t.len = t.ptab + (mixed ? kPhaseTabBytes : 0);
+    t.len = t.ptab + kPhaseTabBytes;  // mixed: int4 entries; FP64: double2 entries
     t.maxl = t.len + (size_t)cchunk * nl_pad * 8;
     t.cbin = t.maxl + (size_t)cchunk * 4;
     t.total = (t.cbin + (size_t)cchunk * 4 + 15) / 16 * 16;
@@ -311,7 +312,6 @@ __device__ __forceinline__ void add_rates(const TileJob& j, int ci, int e, const
 
 template <bool MIXED>
 __device__ __forceinline__ void stage_phase_table(unsigned char* smem, const TileSmem& L, const int4* ptab) {
-    if (!MIXED) return;
     const int nt = blockDim.x * blockDim.y, t = threadIdx.y * blockDim.x + threadIdx.x;
     int4* s = (int4*)(smem + L.ptab);
     for (int i = t; i < kPhaseTabN + 1; i += nt) s[i] = ptab[i];
@@ -387,7 +387,7 @@ __device__ __forceinline__ void process_tile(const TileJob& j, int nl, int nl_pa
             }
         } else {
             F64Src<TE> src{(const double*)s_tab + lane, (const double*)s_pe + lane,
-                           (const double*)s_len_raw + (size_t)cl * nl_pad};
+                           (const double*)s_len_raw + (size_t)cl * nl_pad, (const double2*)s_ptab};
             const F64 ar{};
             double pr[9];
             if (MODE == kModeHeights) {
