@@ -105,14 +105,6 @@ struct Q30 {
         i = mad(a1.im, b0.re, i);
         return C{rnd(r), rnd(i)};
     }
-    // c*x + s*y  and  -s*x + c*y  for a real rotation of two complex numbers
-    __device__ __forceinline__ void rot(R c, R s, C& x, C& y) const {
-        const int ns = -s;
-        const C nx{rnd(mad(s, y.re, mulb(c, x.re))), rnd(mad(s, y.im, mulb(c, x.im)))};
-        const C ny{rnd(mad(c, y.re, mulb(ns, x.re))), rnd(mad(c, y.im, mulb(ns, x.im)))};
-        x = nx;
-        y = ny;
-    }
     // |z|^2 exactly, as Q2.60 in 64 bits
     static __device__ __forceinline__ long long norm2(C z) { return mad(z.im, z.im, mul(z.re, z.re)); }
     // Q2.60 probability -> float, one rounding; the completed entries of the
@@ -250,12 +242,6 @@ struct F64 {
         const double re = fma(a0.re, b1.re, -a0.im * b1.im) - fma(a1.re, b0.re, -a1.im * b0.im);
         const double im = fma(a0.re, b1.im, a0.im * b1.re) - fma(a1.re, b0.im, a1.im * b0.re);
         return C{re, -im};
-    }
-    static __device__ __forceinline__ void rot(R c, R s, C& x, C& y) {
-        const C nx{fma(c, x.re, s * y.re), fma(c, x.im, s * y.im)};
-        const C ny{fma(c, y.re, -s * x.re), fma(c, y.im, -s * x.im)};
-        x = nx;
-        y = ny;
     }
     static __device__ __forceinline__ void complete(const C B[4], double out[9]) {
         const double q00 = fma(B[0].re, B[0].re, B[0].im * B[0].im), q01 = fma(B[1].re, B[1].re, B[1].im * B[1].im);

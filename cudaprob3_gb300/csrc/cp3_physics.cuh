@@ -207,15 +207,10 @@ CP3_HD void layer_eigen(const OscParams& p, double E, double rhoye, double m[3],
     }
 }
 
-// Phase rate of eigenvalue k relative to eigenvalue 0, in turns per km:
-// the reference's phase -LoEfac * m_k * L / E (physics.hpp:461-467) with the
-// per-layer common phase of m_0 removed, divided by 2*pi.
-CP3_HD double phase_turns_per_km(double mk, double m0, double E) {
-    return -kLoEfac * (mk - m0) / E / kTwoPi;
-}
-
-// The same with the energy factor -LoEfac / (2 pi E) computed once per
-// (energy, layer): phase_rate_factor(E) * (mk - m0).
+// Phase rate factor of the layer propagator: eigenvalue k's phase relative to
+// eigenvalue 0 is -LoEfac * (m_k - m_0) * L / E (physics.hpp:461-467) with the
+// per-layer common phase of m_0 removed; in turns per km that is
+// phase_rate_factor(E) * (m_k - m_0), the factor computed once per (energy, layer).
 CP3_HD double phase_rate_factor(double E) { return -kLoEfac / (kTwoPi * E); }
 
 // Total path length including the production height (physics.hpp:615-616), cm.
