@@ -228,6 +228,48 @@ def make_prop(cp, precision, cos, en, B, nom, device):
     return p
 
 
+def small_case(cp, dev):
+    """The reference's CPU-runnable case (256 cos x 256 E over 0.5-100 GeV,
+    4-shell body, neutrinos): GPU mixed and FP64 (one calculation, CUDA events
+    on the handle's stream, best of 20) against the CPU port with all host
+    threads (min of 3 after a warm-up) on the whole grid."""
+    import torch
+
+    import oracle
+    from cudaprob3_gb300 import grids as G
+    n = 256
+    cos = G.linspace(-1.0, 0.0, n)
+    en = G.logspace(0.5, 100.0, n)
+    B = G.PREM_4
+    out = {"workload": "256 cos x 256 E (0.5-100 GeV), 4-shell body, nominal parameters, nu"}
+    for precision in ("mixed", "fp64"):
+        p = make_prop(cp, precision, cos, en, B, G.NOMINAL, dev)
+        s = torch.cuda.Stream(device=dev)
+        p.set_stream(s.cuda_stream)
+        best = 1e30
+        for _ in range(20):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(s)
+            p.calculateProbabilitiesAsync(cp.Neutrino)
+            b.record(s)
+            b.synchronize()
+            best = min(best, a.elapsed_time(b))
+        out["gpu_%s_pairs_per_s" % precision] = n * n / (best * 1e-3)
+        p.close()
+    threads = os.cpu_count() or 1
+    oracle.calculate(cos, en, B.radii, B.rho_eff(), G.NOMINAL, 22.0, False, threads=threads)
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        oracle.calculate(cos, en, B.radii, B.rho_eff(), G.NOMINAL, 22.0, False, threads=threads)
+        ts.append(time.perf_counter() - t0)
+    out["cpu_port_pairs_per_s"] = n * n / min(ts)
+    out["cpu_cores"] = threads
+    out["note"] = "a 65,536-pair grid is launch-bound on the GPU"
+    return out
+
+
 def run_ours(args, world, rank, local):
     import torch
 
@@ -352,22 +394,29 @@ def run_ours(args, world, rank, local):
     en_h = np.ascontiguousarray(en)
     e2e_steps = max(3, min(args.steps, 20))
 
-    def e2e_run(zero_copy):
+    def e2e_run(mode):
+        # mode "memcpy": planes into the handle's device buffer, then one
+        # copy to host; "zero_copy": the kernel stores all nine planes into
+        # page-locked host memory; "block": it stores the four planes of the
+        # 2x2 flavour block there and waitForCompletion derives the other
+        # five on the host cores (set_host_completion)
         for (p, _), h in zip(props, host):
             p.set_stream(0)  # each handle on its own stream
-            if zero_copy:
-                p.set_host_result_buffer(h.data_ptr(), h.numel() * 4)
-            else:
+            if mode == "memcpy":
                 p.set_result_buffer(0, 0)
+            else:
+                p.set_host_result_buffer(h.data_ptr(), h.numel() * 4)
+            p.set_host_completion(mode == "block")
         for (p, t), h in zip(props, host):  # warm-up
             p.calculateProbabilities(t)
         barrier(world)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            if zero_copy:
+            if mode != "memcpy":
                 # both types in flight on their own streams, one wait each:
-                # the second's uploads and prep overlap the first's stores
+                # the second's uploads and prep overlap the first's stores,
+                # its stores overlap the first's host completion
                 for (p, t), h in zip(props, host):
                     p.setEnergyList(en_h)
                     p.setCosineList(cos_h)
@@ -381,19 +430,33 @@ def run_ours(args, world, rank, local):
                     p.calculateProbabilities(t)
                     p.copy_results_to(h.data_ptr(), h.numel() * 4)
         torch.cuda.synchronize()
+        dt = allmax(world, (time.perf_counter() - t0) / e2e_steps)
         for i, (p, _) in enumerate(props):
+            p.set_host_completion(False)
             p.set_stream(streams[i].cuda_stream)
-        return allmax(world, (time.perf_counter() - t0) / e2e_steps)
+        return dt
 
-    e2e_memcpy_s = e2e_run(False)
-    e2e_s = e2e_run(True)
+    e2e_memcpy_s = e2e_run("memcpy")
+    e2e_block_s = e2e_run("block")
+    e2e_s = e2e_run("zero_copy")
+    # the host planes of the last e2e step against the device planes of the
+    # timed steps (same inputs)
+    e2e_dp = max(float((h.to(buf.device) - buf).abs().max()) for h, buf in zip(host, bufs))
+    plane_bytes = NC * NE * 4
     e2e = {"value": world * pairs_step / e2e_s, "unit": "pairs/s",
            "h2d_bytes_per_step": 2 * 8 * (NC + NE), "d2h_bytes_per_step": 2 * out_bytes,
            "ms_per_step": e2e_s * 1e3,
-           "d2h": "kernel stores into page-locked host buffers (set_host_result_buffer); host-timed "
-                  "setEnergyList + setCosineList + calculateProbabilitiesAsync per type on the handles' own "
-                  "streams, then waitForCompletion",
-           "copy_after_kernel": {"value": world * pairs_step / e2e_memcpy_s, "ms_per_step": e2e_memcpy_s * 1e3}}
+           "d2h": "the kernel stores the nine planes into page-locked host buffers (set_host_result_buffer); "
+                  "host-timed setEnergyList + setCosineList + calculateProbabilitiesAsync per type on the "
+                  "handles' own streams, then waitForCompletion",
+           "max_abs_dp_host_vs_device_planes": e2e_dp,
+           "copy_after_kernel": {"value": world * pairs_step / e2e_memcpy_s, "ms_per_step": e2e_memcpy_s * 1e3,
+                                 "d2h_bytes_per_step": 2 * out_bytes},
+           "block_with_host_completion": {
+               "value": world * pairs_step / e2e_block_s, "ms_per_step": e2e_block_s * 1e3,
+               "d2h_bytes_per_step": 2 * 4 * plane_bytes,
+               "note": "four planes over the link, five derived on the host cores (set_host_completion): "
+                       "host-memory-bound on this box's cores"}}
     for (p, _), buf in zip(props, bufs):
         p.set_result_buffer(buf.data_ptr(), buf.numel() * 4)
 
@@ -451,9 +514,11 @@ def run_ours(args, world, rank, local):
         prec["oracle_subset"] = "every 32nd cosine x every 32nd energy (128 x 128), nu and nubar"
 
     cpu = None
+    configs0 = None
     if rank == 0 and world == 1:
         v, thr, desc = cpu_sample(args.cpu_seconds)
         cpu = {"value": v, "unit": "pairs/s", "cores": thr, "kind": "port", "sample": desc}
+        configs0 = small_case(cp, dev)
 
     if rank == 0:
         line = {
@@ -471,6 +536,7 @@ def run_ours(args, world, rank, local):
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clocks, "fp64": fp64, "precision": prec,
             "speedup_vs_fp64": (value / fp64["value"]) if fp64 else None,
+            "configs0": configs0,
         }
         print(json.dumps(line), flush=True)
     for p, _ in props:

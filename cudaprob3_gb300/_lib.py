@@ -51,6 +51,7 @@ SIGNATURES = [
     ("cp3_copy_results_to_host", _I, [_P, _P, _SZ]),
     ("cp3_set_result_buffer", _I, [_P, _P, _SZ]),
     ("cp3_set_host_result_buffer", _I, [_P, _P, _SZ]),
+    ("cp3_set_host_completion", _I, [_P, _I]),
     ("cp3_set_rate_flux", _I, [_P, _P, _I, _I]),
     ("cp3_set_rate_bins", _I, [_P, _IP, _IP, _I, _I]),
     ("cp3_calculate_rates", _I, [_P, _I]),

@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcudaprob3_gb300.so")
 SOURCES = ["cp3_abi.cu", "cp3_kernels.cu", "cp3_pipes.cu", "cp3_batch.cu", "cp3_loglik.cu", "cp3_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr",
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-fopenmp", "--expt-relaxed-constexpr",
               "-I" + os.path.join(ROOT, "include")]
 
 
@@ -72,7 +72,7 @@ def build(verbose=False, force=False):
     with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         list(ex.map(run, jobs))
     if force or jobs or not _newer(LIB, objs) or not _loads_here(LIB):
-        run([nvcc()] + ARCH + ["-shared", "-o", LIB] + objs)
+        run([nvcc()] + ARCH + ["-shared", "-Xcompiler", "-fopenmp", "-o", LIB] + objs)
     return LIB
 
 

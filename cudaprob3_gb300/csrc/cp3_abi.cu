@@ -92,6 +92,8 @@ struct cp3_propagator {
     void* ext_result = nullptr;
     size_t ext_bytes = 0;
     void* ext_host = nullptr;  // caller page-locked host buffer behind ext_result (zero-copy)
+    bool host_completion = false;  // with ext_host: store the 2x2 block, derive the rest on the host
+    bool completion_pending = false;
 
     // fused event rates
     DevBuf<float> d_flux;
@@ -144,6 +146,37 @@ void set_maxlayers(cp3_propagator* p) {
 int check(cp3_propagator* p) {
     if (!p) return fail(CP3_ERR_ARGUMENT, "null propagator handle");
     return CP3_OK;
+}
+
+}  // namespace
+
+namespace {
+
+// The five planes that unitarity fixes, from the four of the 2x2 flavour
+// block stored by the kernel (planes in*3+out: rows and columns of the 3x3
+// probability matrix sum to one), on the host cores; doubles inside, one
+// rounding to the plane type, clamped at zero like the kernel's completion.
+template <class T>
+void complete_planes_on_host(T* h, size_t plane) {
+    T* p0 = h;
+    T* p1 = h + plane;
+    T* p2 = h + 2 * plane;
+    T* p3 = h + 3 * plane;
+    T* p4 = h + 4 * plane;
+    T* p5 = h + 5 * plane;
+    T* p6 = h + 6 * plane;
+    T* p7 = h + 7 * plane;
+    T* p8 = h + 8 * plane;
+    const long long n = (long long)plane;
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < n; i++) {
+        const double ee = p0[i], em = p1[i], me = p3[i], mm = p4[i];
+        p2[i] = (T)std::max(0.0, 1.0 - ee - em);  // e -> tau
+        p5[i] = (T)std::max(0.0, 1.0 - me - mm);  // mu -> tau
+        p6[i] = (T)std::max(0.0, 1.0 - ee - me);  // tau -> e
+        p7[i] = (T)std::max(0.0, 1.0 - em - mm);  // tau -> mu
+        p8[i] = (T)std::max(0.0, ee + em + me + mm - 1.0);  // tau -> tau
+    }
 }
 
 }  // namespace
@@ -410,6 +443,7 @@ int cp3_set_result_buffer(cp3_propagator* p, void* dptr, size_t bytes) {
     p->ext_result = dptr;
     p->ext_bytes = dptr ? bytes : 0;
     p->ext_host = nullptr;
+    p->completion_pending = false;
     p->results_on_host = false;
     return CP3_OK;
 }
@@ -455,8 +489,9 @@ int calc_async(cp3_propagator* p, int type, bool rates) {
         return fail(CP3_ERR_ARGUMENT, "calculateProbabilities: unknown neutrino type");
     if (rates && p->n_h > 1)
         return fail(CP3_ERR_STATE, "calculateRates: not available with a production-height distribution");
-    const int mode = rates ? 1 : (p->n_h > 1 ? 2 : 0);
+    const int mode = rates ? 1 : (p->n_h > 1 ? 2 : (p->ext_host && p->host_completion ? 3 : 0));
     if (!rates) p->results_on_host = false;
+    p->completion_pending = (mode == 3);
     p->last_launches = 0;
     if (p->n_cos == 0 || p->n_en == 0) return CP3_OK;
     DeviceGuard g(p->device);
@@ -734,6 +769,20 @@ int cp3_wait_for_completion(cp3_propagator* p) {
     DeviceGuard g(p->device);
     cudaError_t e = cudaStreamSynchronize(p->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+    if (p->completion_pending) {
+        const size_t plane = (size_t)p->n_cos * p->n_en;
+        if (p->mixed)
+            complete_planes_on_host((float*)p->ext_host, plane);
+        else
+            complete_planes_on_host((double*)p->ext_host, plane);
+        p->completion_pending = false;
+    }
+    return CP3_OK;
+}
+
+int cp3_set_host_completion(cp3_propagator* p, int enable) {
+    if (int rc = check(p)) return rc;
+    p->host_completion = enable != 0;
     return CP3_OK;
 }
 

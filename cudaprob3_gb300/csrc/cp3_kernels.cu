@@ -170,6 +170,7 @@ cudaError_t launch_propagate(bool mixed, const PropArgs& a, int te, int groups, 
     if (a.n_cos == 0 || a.n_en == 0) return cudaSuccess;
     if (mode == kModeRates) return launch_prop_r<kModeRates>(mixed, a, te, groups, smem, s);
     if (mode == kModeHeights) return launch_prop_r<kModeHeights>(mixed, a, te, groups, smem, s);
+    if (mode == kModeBlock) return launch_prop_r<kModeBlock>(mixed, a, te, groups, smem, s);
     return launch_prop_r<kModePlanes>(mixed, a, te, groups, smem, s);
 }
 

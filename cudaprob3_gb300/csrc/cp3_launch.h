@@ -54,7 +54,8 @@ int max_dynamic_smem();
 // Largest block (threads) the propagate kernel of a precision accepts.
 inline int propagate_max_threads(bool mixed) { return mixed ? 256 : 128; }
 cudaError_t launch_prep(bool mixed, PrepArgs a, cudaStream_t s);
-// mode: 0 planes, 1 fused rates, 2 planes averaged over production heights
+// mode: 0 planes, 1 fused rates, 2 planes averaged over production heights,
+// 3 the four planes of the 2x2 flavour block only
 cudaError_t launch_propagate(bool mixed, const PropArgs& a, int te, int groups, size_t smem,
                              cudaStream_t s, int mode = 0);
 

@@ -257,6 +257,8 @@ struct TileJob {
 constexpr int kModePlanes = 0;   // store the nine planes
 constexpr int kModeRates = 1;    // fused event-rate histograms
 constexpr int kModeHeights = 2;  // planes averaged over production heights
+constexpr int kModeBlock = 3;    // only the planes of the 2x2 flavour block (e->e, e->mu, mu->e, mu->mu);
+                                 // the host derives the other five (unitarity)
 
 // Adds one run of rates (the lanes' sums since the warp's cosine bin `cb`
 // changed) to the histogram.  `cb` is warp-uniform (a warp's lanes share the
@@ -382,8 +384,15 @@ __device__ __forceinline__ void process_tile(const TileJob& j, int nl, int nl_pa
                 if (cb >= 0 && my_eb >= 0) add_rates(j, ci, e, pr, r0, r1, r2);
             } else if (store) {
                 float* out = (float*)j.out + (size_t)ci * j.n_en + e;
+                if (MODE == kModeBlock) {
+                    __stcs(out, pr[0]);
+                    __stcs(out + plane, pr[1]);
+                    __stcs(out + 3 * plane, pr[3]);
+                    __stcs(out + 4 * plane, pr[4]);
+                } else {
 #pragma unroll
-                for (int t = 0; t < 9; t++) __stcs(out + (size_t)t * plane, pr[t]);
+                    for (int t = 0; t < 9; t++) __stcs(out + (size_t)t * plane, pr[t]);
+                }
             }
         } else {
             F64Src<TE> src{(const double*)s_tab + lane, (const double*)s_pe + lane,
@@ -407,8 +416,15 @@ __device__ __forceinline__ void process_tile(const TileJob& j, int nl, int nl_pa
                 if (cb >= 0 && my_eb >= 0) add_rates(j, ci, e, pr, r0, r1, r2);
             } else if (store) {
                 double* out = (double*)j.out + (size_t)ci * j.n_en + e;
+                if (MODE == kModeBlock) {
+                    __stcs(out, pr[0]);
+                    __stcs(out + plane, pr[1]);
+                    __stcs(out + 3 * plane, pr[3]);
+                    __stcs(out + 4 * plane, pr[4]);
+                } else {
 #pragma unroll
-                for (int t = 0; t < 9; t++) __stcs(out + (size_t)t * plane, pr[t]);
+                    for (int t = 0; t < 9; t++) __stcs(out + (size_t)t * plane, pr[t]);
+                }
             }
         }
     }

@@ -232,6 +232,12 @@ class CudaPropagatorSingle:
         check(self._lib.cp3_rates_device_ptr(self._h, ctypes.byref(p)))
         return p.value
 
+    def set_host_completion(self, enable=True):
+        """With a host result buffer: the kernel stores the four planes of the
+        2x2 flavour block and waitForCompletion derives the other five on the
+        host cores (4/9 of the bytes over the host link)."""
+        check(self._lib.cp3_set_host_completion(self._h, 1 if enable else 0))
+
     def set_stream(self, stream_handle):
         check(self._lib.cp3_set_stream(self._h, ctypes.c_void_p(stream_handle)))
 

@@ -134,6 +134,9 @@ public:
     void setHostResultBuffer(FLOAT_T* host, size_t elements) {
         detail::check(cp3_set_host_result_buffer(alive(), host, elements * sizeof(FLOAT_T)));
     }
+    /// With a host result buffer: store the 2x2 flavour block only and derive
+    /// the other five planes on the host cores in waitForCompletion.
+    void setHostCompletion(bool enable) { detail::check(cp3_set_host_completion(alive(), enable ? 1 : 0)); }
     /// Production-height distribution (no reference counterpart): the
     /// probabilities are averaged over the heights (km) with the weights
     /// (normalised); setProductionHeight ends the distribution.

@@ -151,6 +151,17 @@ int cp3_set_result_buffer(cp3_propagator* p, void* dptr, size_t bytes);
  * returns to the handle's own device buffer. */
 int cp3_set_host_result_buffer(cp3_propagator* p, void* host, size_t bytes);
 
+/* With a host result buffer: enable = 1 makes the kernel store only the four
+ * planes of the 2x2 flavour block (e->e, e->mu, mu->e, mu->mu: 4/9 of the
+ * bytes over the host link) and cp3_wait_for_completion derive the other five
+ * on the host cores from unitarity (rows and columns sum to one; in double,
+ * one rounding, clamped at zero).  The four stored planes are the kernel's;
+ * the derived ones differ from the device completion by a few units of the
+ * last place.  No effect without a host result buffer, with fused rates or
+ * with a production-height distribution.  Default 0.  (No reference
+ * counterpart.) */
+int cp3_set_host_completion(cp3_propagator* p, int enable);
+
 /* ---- Fused event rates (no reference counterpart) -------------------------
  * The reference's caller reads all nine planes back (getProbability,
  * cudapropagator.cuh:168-181) to weight events.  These entry points do that

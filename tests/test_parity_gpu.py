@@ -212,6 +212,43 @@ def test_host_result_buffer_zero_copy(gpu, precision):
         assert not np.array_equal(p.results(), own)
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_host_completion(gpu, precision):
+    """The kernel stores the 2x2 block into host memory, the host derives the
+    other five planes: the stored planes are the kernel's bits, the derived
+    ones within a few ulp of the device completion (1e-15 FP64, 3e-7 mixed),
+    rows and columns sum to one."""
+    torch = pytest.importorskip("torch")
+    c = G.linspace(-1, 1, 96)
+    e = G.logspace(0.1, 1000, 144)
+    dt = torch.float32 if precision == "mixed" else torch.float64
+    with make(gpu, precision, c, e, G.PREM_12.radii, G.PREM_12.rhos, G.PREM_12.ye, G.NOMINAL) as p:
+        p.calculateProbabilities(gpu.Neutrino)
+        own = p.results()
+        host = torch.full((9, 96, 144), -1.0, dtype=dt).pin_memory()
+        p.set_host_result_buffer(host.data_ptr(), host.numel() * host.element_size())
+        p.set_host_completion(True)
+        p.calculateProbabilitiesAsync(gpu.Neutrino)
+        p.waitForCompletion()
+        got = host.numpy()
+        for t in (0, 1, 3, 4):
+            assert np.array_equal(got[t], own[t])
+        tol = 3e-7 if precision == "mixed" else 1e-15
+        assert np.abs(got.astype(np.float64) - own).max() <= tol
+        s = got.astype(np.float64).reshape(3, 3, 96, 144)
+        assert np.abs(s.sum(axis=0) - 1).max() <= 4 * tol and np.abs(s.sum(axis=1) - 1).max() <= 4 * tol
+        # getProbability of a derived plane after a synchronous calculation
+        host.fill_(-1.0)
+        p.calculateProbabilities(gpu.Antineutrino)
+        assert p.getProbability(40, 70, gpu.ProbType.t_t) == float(host.numpy()[8, 40, 70])
+        assert host.numpy().min() >= 0.0
+        # off again: every plane from the kernel
+        p.set_host_completion(False)
+        p.calculateProbabilities(gpu.Neutrino)
+        assert np.array_equal(host.numpy(), own)
+        p.set_host_result_buffer(0, 0)
+
+
 def test_configs1_scale_mixed_vs_fp64(gpu):
     """4096 x 4096 grid, 0.1-1000 GeV, 11-shell body: the mixed kernel against
     the FP64 kernel on every pair (device-side comparison) and against the
