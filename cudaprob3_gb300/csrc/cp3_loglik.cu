@@ -18,12 +18,16 @@
 //                     matrix from the tables (no per-layer storage: the chain is
 //                     un-multiplied with T^T and conj(D)); per-(energy, layer)
 //                     adjoints are summed over the warp's cosines with shuffles
-//   ll_layer_kernel   one block per energy, three threads (rows) per layer:
-//                     sums the warps' partials and back-propagates through the
-//                     layer's FP64 eigen-decomposition to the parameters
-//   ll_sum_kernel     sums the per-energy rows (fixed order: deterministic)
+//   ll_layer_kernel   three threads (rows) per (energy, layer), packed densely
+//                     over energies: sums the warps' partials and
+//                     back-propagates through the layer's FP64
+//                     eigen-decomposition to the parameters
+//   ll_sum_kernel     one block per output: sums the per-energy rows (fixed
+//                     order: deterministic)
 // Precision: FP64 does every step in double; MIXED runs ll_pair_kernel in
-// FP32 (phases in double-float) with the FP64 tables and FP64 reduction.
+// FP32 (phases in double-float) with the FP64 tables, sums its float partials
+// over the cosine chunks by compensated FP32 sums and does the eigen
+// back-propagation in FP64.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -99,6 +103,7 @@ __device__ __forceinline__ Cx<float> phase_of(float2 kap, float2 L) {
 struct LLArgs {
     // inputs on the device
     const OscParams* osc;
+    const double* cmat;     // [4][3][3]: dH/d(theta12, theta13, dm21, dm32) of H = O diag(0, d1, d2) O^T
     const double* rhoye;    // [nl]
     const double* energies; // [n_en]
     const double* cosines;  // [n_cos]
@@ -115,8 +120,8 @@ struct LLArgs {
     double* pe;
     double* len;
     // partials and results
-    double* part_l;  // [n_cchunk][n_en][nl][11] (FP64 kernel)
-    double* part_e;  // [n_cchunk][n_en][19]
+    double* part_l;  // [n_en][nl][n_cchunk][11] (FP64 kernel)
+    double* part_e;  // [n_en][n_cchunk][19]
     float* part_l_f; // the same in float for the mixed kernel (null for FP64)
     float* part_e_f;
     // float copies of the inputs for the mixed kernel
@@ -467,8 +472,11 @@ __global__ void __launch_bounds__(128) ll_pair_kernel(LLArgs a) {
 
     // per-(energy, layer) partials: layers Mw .. 1 (descending), then layer 0
     // partials in the kernel's precision (float buffers for the mixed kernel)
+    // layout [energy][layer][cosine chunk][11]: a layer's partials are one
+    // contiguous block for the layer kernel
+    const size_t lstride = (size_t)a.n_cchunk * kLLPerL;
     R* pl = (R*)(std::is_same<R, float>::value ? (void*)a.part_l_f : (void*)a.part_l) +
-            ((size_t)cchunk * a.n_en + e) * a.nl * kLLPerL;
+            (size_t)e * a.nl * lstride + (size_t)cchunk * kLLPerL;
     for (int l = Mw; l >= 1; l--) {
         R tT[9];
         R tk[2] = {0, 0};
@@ -525,18 +533,18 @@ __global__ void __launch_bounds__(128) ll_pair_kernel(LLArgs a) {
 #pragma unroll
         for (int q = 0; q < 9; q++) {
             const R v = warp_sum(tT[q]);
-            if (lane == 0) pl[(size_t)l * kLLPerL + q] = v;
+            if (lane == 0) pl[(size_t)l * lstride + q] = v;
         }
 #pragma unroll
         for (int k = 0; k < 2; k++) {
             const R v = warp_sum(tk[k]);
-            if (lane == 0) pl[(size_t)l * kLLPerL + 9 + k] = v;
+            if (lane == 0) pl[(size_t)l * lstride + 9 + k] = v;
         }
     }
     // layers above Mw are never crossed by this warp's cosines
     if (lane == 0)
         for (int l = Mw + 1; l < a.nl; l++)
-            for (int q = 0; q < kLLPerL; q++) pl[(size_t)l * kLLPerL + q] = R(0);
+            for (int q = 0; q < kLLPerL; q++) pl[(size_t)l * lstride + q] = R(0);
     // layer 0: T_0 and D_0
     {
 #pragma unroll
@@ -552,7 +560,7 @@ __global__ void __launch_bounds__(128) ll_pair_kernel(LLArgs a) {
     }
     // per energy: Lambda', Gamma', LL
     R* pe = (R*)(std::is_same<R, float>::value ? (void*)a.part_e_f : (void*)a.part_e) +
-            ((size_t)cchunk * a.n_en + e) * kLLPerE;
+            ((size_t)e * a.n_cchunk + cchunk) * kLLPerE;
     R vals[kLLPerE - 1];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
@@ -577,15 +585,39 @@ __global__ void __launch_bounds__(128) ll_pair_kernel(LLArgs a) {
 // theta23, dCP, dm12sq, dm23sq, [7 + r] density of the caller's row r.
 constexpr int kLLOscOut = 7;
 
-// Lanes per row group of ll_layer_kernel: the layers rounded up to a warp.
-__host__ __device__ inline int ll_layer_lanes(int nl) { return (nl + 31) / 32 * 32; }
+// Items of ll_layer_kernel: (energy slot, row r, layer l), 3 nl per energy,
+// packed densely (the FP64 pipe is paid per warp instruction, whatever the
+// active lanes), epb energies per block.
+__host__ __device__ inline int ll_layer_threads(int nl, int epb) { return (epb * 3 * nl + 31) / 32 * 32; }
+__host__ __device__ inline int ll_layer_slot_doubles(int nl) {
+    return nl * (9 + 9 + 2 + 3 + 3 + 9) + kLLPerE + 3 * nl * kLLOscOut + 3 * kLLOscOut;
+}
 
-// Block e: energy e.  Thread (r, l) = (threadIdx.x / S, threadIdx.x % S),
-// S = ll_layer_lanes(nl), handles row r in {0, 1, 2} of the 3x3 quantities of
-// layer l < nl, so that the FP64 chain of each (energy, layer) is split
-// three ways (the work is 2 x 10^3 short chains: latency, not throughput):
-//   1. sums of the warps' partials (11 per layer) and the eigen-pairs solved by
-//      the prep kernel, into shared memory;
+// Cosine chunks whose partials ll_layer_kernel loads before summing them.
+constexpr int kLLBatch = 8;
+
+// Compensated FP32 sum (Knuth's TwoSum per term): the error of each add is
+// carried in c, so s + c is the sum of the float terms to about 2^-46 of their
+// magnitudes, on the FP32 pipe instead of float-to-double conversions and FP64
+// adds.
+struct FloatTwoSum {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        const float t = s + x, bp = t - s;
+        c += (s - (t - bp)) + (x - bp);
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
+// Item (slot, r, l) of block b: energy b * epb + slot, row r in {0, 1, 2} of
+// the 3x3 quantities of layer l, so that the FP64 chain of each (energy,
+// layer) is split three ways (the work is 2 x 10^3 short chains, bound by the
+// FP64 issue of the busiest SM, not by the GPU's FP64 throughput):
+//   1. sums of the warps' partials (11 per layer; the mixed kernel's float
+//      partials by compensated FP32 sums), the eigen-pairs solved
+//      by the prep kernel and one reciprocal eigenvalue gap per row, into
+//      shared memory;
 //   2. row r of the eigenvector adjoint gV_l from the two overlaps the layer
 //      enters (T_{l-1} = V_l^T V_{l-1}, T_l = V_{l+1}^T V_l) and, for l = 0, 1,
 //      from Gamma' / Lambda';
@@ -593,59 +625,122 @@ __host__ __device__ inline int ll_layer_lanes(int nl) { return (nl + 31) / 32 * 
 //      dLL/dm_k on it (symmetric eigenvector adjoint);
 //   4. row r of gH = V W V^T;
 //   5. row r's share of the contractions of sym(gH) with the parameter
-//      derivatives of H_l = O diag(0, d1, d2) O^T - fac_l e0 e0^T.
+//      derivatives of H_l = O diag(0, d1, d2) O^T - fac_l e0 e0^T: cmat holds
+//      the four symmetrised 3x3 derivative matrices (theta12, theta13, dm21,
+//      dm32), formed on the host with the parameters, so the contraction is
+//      sum_q gH[r][q] C[r][q].
 // Densities map one-to-one to layers (single writer per slot); the
-// oscillation parameters are summed over the block in a fixed order.
-__global__ void __launch_bounds__(288) ll_layer_kernel(LLArgs a) {
+// oscillation parameters of an energy are summed over its items in a fixed
+// order (rows' layers, then the three rows).
+__global__ void __launch_bounds__(288) ll_layer_kernel(LLArgs a, int epb) {
     extern __shared__ double s_ll[];
-    const int nl = a.nl, S = ll_layer_lanes(nl);
-    const int r = threadIdx.x / S, l = threadIdx.x % S;
-    const int e = blockIdx.x;
-    double* sV = s_ll;                 // [nl][9]
+    const int nl = a.nl, per = 3 * nl;
+    const int slot = threadIdx.x / per, w = threadIdx.x - slot * per;
+    const int r = w / nl, l = w - r * nl;
+    const int e = blockIdx.x * epb + slot;
+    const bool live = slot < epb && e < a.n_en;
+    double* sV = s_ll + (size_t)(slot < epb ? slot : 0) * ll_layer_slot_doubles(nl);  // [nl][9]
     double* sT = sV + nl * 9;          // [nl][9] summed adjoint of T_l
     double* sK = sT + nl * 9;          // [nl][2] summed adjoint of kappa_l
     double* sM = sK + nl * 2;          // [nl][3] eigenvalues
-    double* sG = sM + nl * 3;          // [nl][9] gV, then W, then gH
+    double* sI = sM + nl * 3;          // [nl][3] 1 / (m_{r+1} - m_{r+2}), indices mod 3
+    double* sG = sI + nl * 3;          // [nl][9] gV, then W
     double* sL = sG + nl * 9;          // [19]
-    double* sRed = sL + kLLPerE;       // [blockDim / 32][7]
+    double* sAcc = sL + kLLPerE;       // [3 nl][7]
+    double* sRow = sAcc + per * kLLOscOut;  // [3][7]
     const OscParams& o = *a.osc;
-    const double E = a.energies[e];
-    const bool live = l < nl;
-    // 1. partial sums (float from the mixed pair kernel), eigen-pairs
+    const double E = live ? a.energies[e] : 1.0;
+    // 1. partial sums, eigen-pairs, reciprocal gaps.  The partials are read
+    // kLLBatch chunks at a time with every load of a batch issued before the
+    // first add (one memory round trip per batch, not per chunk).
     if (live) {
-        for (int q = r; q < kLLPerL; q += 3) {
-            double v = 0.0;
-            for (int cc = 0; cc < a.n_cchunk; cc++) {
-                const size_t i = (((size_t)cc * a.n_en + e) * nl + l) * kLLPerL + q;
-                v += a.part_l_f ? (double)a.part_l_f[i] : a.part_l[i];
-            }
-            if (q < 9)
-                sT[l * 9 + q] = v;
-            else
-                sK[l * 2 + q - 9] = v;
-        }
         const double* ev = a.eig + ((size_t)e * nl + l) * kLLEigWords;
+        const int r1 = (r == 2) ? 0 : r + 1, r2 = (r == 0) ? 2 : r - 1;
+        double vr[3];
 #pragma unroll
-        for (int k = 0; k < 3; k++) sV[l * 9 + 3 * r + k] = ev[3 * r + k];
-        sM[l * 3 + r] = ev[9 + r];
-    }
-    for (int w = threadIdx.x; w < kLLPerE; w += blockDim.x) {
-        double v = 0.0;
-        for (int cc = 0; cc < a.n_cchunk; cc++) {
-            const size_t i = ((size_t)cc * a.n_en + e) * kLLPerE + w;
-            v += a.part_e_f ? (double)a.part_e_f[i] : a.part_e[i];
+        for (int k = 0; k < 3; k++) vr[k] = ev[3 * r + k];
+        const double mr = ev[9 + r], m1 = ev[9 + r1], m2 = ev[9 + r2];
+        const size_t lb = ((size_t)e * nl + l) * a.n_cchunk * kLLPerL + r;  // this layer's block, q = r
+        const int nq = (r < 2) ? 4 : 3;                                    // q = r + 3 i < 11
+        double v[4];
+        if (a.part_l_f) {
+            FloatTwoSum f[4];
+            for (int c0 = 0; c0 < a.n_cchunk; c0 += kLLBatch) {
+                float x[kLLBatch][4];
+#pragma unroll
+                for (int u = 0; u < kLLBatch; u++)
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+                        x[u][i] = (c0 + u < a.n_cchunk && i < nq) ? a.part_l_f[lb + (size_t)(c0 + u) * kLLPerL + 3 * i] : 0.0f;
+#pragma unroll
+                for (int u = 0; u < kLLBatch; u++)
+#pragma unroll
+                    for (int i = 0; i < 4; i++) f[i].add(x[u][i]);
+            }
+#pragma unroll
+            for (int i = 0; i < 4; i++) v[i] = f[i].value();
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; i++) v[i] = 0.0;
+            for (int c0 = 0; c0 < a.n_cchunk; c0 += kLLBatch) {
+                double x[kLLBatch][4];
+#pragma unroll
+                for (int u = 0; u < kLLBatch; u++)
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+                        x[u][i] = (c0 + u < a.n_cchunk && i < nq) ? a.part_l[lb + (size_t)(c0 + u) * kLLPerL + 3 * i] : 0.0;
+#pragma unroll
+                for (int u = 0; u < kLLBatch; u++)
+#pragma unroll
+                    for (int i = 0; i < 4; i++) v[i] += x[u][i];
+            }
         }
-        sL[w] = v;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int q = r + 3 * i;
+            if (q < 9)
+                sT[l * 9 + q] = v[i];
+            else if (q < kLLPerL)
+                sK[l * 2 + q - 9] = v[i];
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++) sV[l * 9 + 3 * r + k] = vr[k];
+        sM[l * 3 + r] = mr;
+        const double gap = m1 - m2;
+        sI[l * 3 + r] = (gap != 0.0) ? 1.0 / gap : 0.0;
+        for (int q = w; q < kLLPerE; q += per) {
+            const size_t pb = (size_t)e * a.n_cchunk * kLLPerE + q;
+            double sum = 0.0;
+            if (a.part_e_f) {
+                FloatTwoSum f;
+                for (int c0 = 0; c0 < a.n_cchunk; c0 += kLLBatch) {
+                    float x[kLLBatch];
+#pragma unroll
+                    for (int u = 0; u < kLLBatch; u++) x[u] = (c0 + u < a.n_cchunk) ? a.part_e_f[pb + (size_t)(c0 + u) * kLLPerE] : 0.0f;
+#pragma unroll
+                    for (int u = 0; u < kLLBatch; u++) f.add(x[u]);
+                }
+                sum = f.value();
+            } else {
+                for (int c0 = 0; c0 < a.n_cchunk; c0 += kLLBatch) {
+                    double x[kLLBatch];
+#pragma unroll
+                    for (int u = 0; u < kLLBatch; u++) x[u] = (c0 + u < a.n_cchunk) ? a.part_e[pb + (size_t)(c0 + u) * kLLPerE] : 0.0;
+#pragma unroll
+                    for (int u = 0; u < kLLBatch; u++) sum += x[u];
+                }
+            }
+            sL[q] = sum;
+        }
     }
     __syncthreads();
 
     double acc[kLLOscOut];
 #pragma unroll
     for (int q = 0; q < kLLOscOut; q++) acc[q] = 0.0;
-    const double s23 = o.s23, c23 = o.c23, sd = o.sd, cd = o.cd;
     // 2. row r of gV_l
-    double gvr[3] = {0.0, 0.0, 0.0};
     if (live) {
+        double gvr[3] = {0.0, 0.0, 0.0};
         // T_l = V_{l+1}^T V_l: dT_l[i][c] / dV_l[r][c] = V_{l+1}[r][i]
         if (l + 1 < nl)
 #pragma unroll
@@ -661,6 +756,7 @@ __global__ void __launch_bounds__(288) ll_layer_kernel(LLArgs a) {
         if (l <= 1) {
             // l = 1, Lambda' from V_1: row 0 = V_1[0][k]; row 1 = c23 V_1[1][k] + s23 e^{i d} V_1[2][k]
             // l = 0, Gamma' from V_0: column 0 = V_0[0][k]; column 1 = c23 V_0[1][k] + s23 e^{-i d} V_0[2][k]
+            const double s23 = o.s23, c23 = o.c23, sd = o.sd, cd = o.cd;
             const int off = (l == 1) ? 0 : 9;
             const double sg = (l == 1) ? 1.0 : -1.0;
 #pragma unroll
@@ -678,13 +774,11 @@ __global__ void __launch_bounds__(288) ll_layer_kernel(LLArgs a) {
             }
             if (l == 0 && r == 0) acc[0] = sL[18];
         }
-    }
-    __syncthreads();  // sG free (never read before): write gV
-    if (live)
 #pragma unroll
         for (int c = 0; c < 3; c++) sG[l * 9 + 3 * r + c] = gvr[c];
+    }
     __syncthreads();
-    // 3. row j = r of W
+    // 3. row j = r of W; 1 / (m_k - m_r) = +-sI[t], t the third index
     double wr[3];
     if (live) {
         const double f = phase_rate_factor(E);
@@ -698,8 +792,9 @@ __global__ void __launch_bounds__(288) ll_layer_kernel(LLArgs a) {
                 double dot = 0.0;
 #pragma unroll
                 for (int q = 0; q < 3; q++) dot += sV[l * 9 + 3 * q + r] * sG[l * 9 + 3 * q + k];
-                const double gap = sM[l * 3 + k] - sM[l * 3 + r];
-                wr[k] = (gap != 0.0) ? dot / gap : 0.0;
+                const int t = 3 - k - r;
+                const double inv = sI[l * 3 + t];
+                wr[k] = dot * (((t == 2 ? 0 : t + 1) == k) ? inv : -inv);
             }
         }
     }
@@ -708,10 +803,9 @@ __global__ void __launch_bounds__(288) ll_layer_kernel(LLArgs a) {
 #pragma unroll
         for (int k = 0; k < 3; k++) sG[l * 9 + 3 * r + k] = wr[k];
     __syncthreads();
-    // 4. row p = r of gH = V W V^T: u_k = sum_j V[r][j] W[j][k], gH[r][q] = sum_k u_k V[q][k]
-    double hr[3] = {0.0, 0.0, 0.0};
     if (live) {
-        double u[3] = {0.0, 0.0, 0.0};
+        // 4. row p = r of gH = V W V^T: u_k = sum_j V[r][j] W[j][k], gH[r][q] = sum_k u_k V[q][k]
+        double u[3] = {0.0, 0.0, 0.0}, hr[3] = {0.0, 0.0, 0.0};
 #pragma unroll
         for (int k = 0; k < 3; k++)
 #pragma unroll
@@ -720,73 +814,52 @@ __global__ void __launch_bounds__(288) ll_layer_kernel(LLArgs a) {
         for (int q = 0; q < 3; q++)
 #pragma unroll
             for (int k = 0; k < 3; k++) hr[q] += u[k] * sV[l * 9 + 3 * q + k];
-    }
-    __syncthreads();
-    if (live)
-#pragma unroll
-        for (int q = 0; q < 3; q++) sG[l * 9 + 3 * r + q] = hr[q];
-    __syncthreads();
-    // 5. contractions of row r of sym(gH)
-    if (live) {
-        const double* O = o.o;
-        const double c13 = O[8], s13 = O[2];
-        const double c12 = (c13 != 0.0) ? O[0] / c13 : O[4];
-        const double sn12 = -O[3];
-        const double dO12[9] = {-c13 * sn12, c13 * c12, 0.0, -c12, -sn12, 0.0, s13 * sn12, -s13 * c12, 0.0};
-        const double dO13[9] = {-s13 * c12, -s13 * sn12, c13, 0.0, 0.0, 0.0, -c13 * c12, -c13 * sn12, -s13};
-        const double dd[3] = {0.0, o.d1, o.d2};
-        double gd1 = 0.0, gd2 = 0.0, gth12 = 0.0, gth13 = 0.0;
+        // 5. contractions of row r of gH with the symmetrised derivative matrices
+        const double* C = a.cmat + 3 * r;
 #pragma unroll
         for (int q = 0; q < 3; q++) {
-            const double h = 0.5 * (sG[l * 9 + 3 * r + q] + sG[l * 9 + 3 * q + r]);
-            // d1, d2: o_1^T gH o_1, o_2^T gH o_2
-            gd1 += h * O[3 * r + 1] * O[3 * q + 1];
-            gd2 += h * O[3 * r + 2] * O[3 * q + 2];
-            // theta12, theta13: 2 tr(gH O D dO^T)
-#pragma unroll
-            for (int k = 1; k < 3; k++) {
-                gth12 += 2.0 * h * O[3 * r + k] * dd[k] * dO12[3 * q + k];
-                gth13 += 2.0 * h * O[3 * r + k] * dd[k] * dO13[3 * q + k];
-            }
+            acc[1] += hr[q] * C[q];
+            acc[2] += hr[q] * C[9 + q];
+            acc[5] += hr[q] * C[18 + q];
+            acc[6] += hr[q] * C[27 + q];
         }
-        acc[1] = gth12;
-        acc[2] = gth13;
-        // d1 = dm12sq, d2 = dm12sq + dm23sq
-        acc[5] = gd1 + gd2;
-        acc[6] = gd2;
         // densities: H[0][0] -= fac, fac = sgn GF E rho Ye
         if (l >= 1 && r == 0) {
             const double sgn = a.anti ? 1.0 : -1.0;
             const int np = 6 + a.n_rows;
-            a.part_g[(size_t)e * (1 + np) + 1 + 6 + a.layer_row[l]] = -sG[l * 9] * sgn * kGF * E * a.ye_layer[l];
+            a.part_g[(size_t)e * (1 + np) + 1 + 6 + a.layer_row[l]] = -hr[0] * sgn * kGF * E * a.ye_layer[l];
         }
-    }
-    // fixed-order sum over the block: warp butterflies, then the warps in order
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-    for (int q = 0; q < kLLOscOut; q++) {
-        const double v = warp_sum(acc[q]);
-        if (lane == 0) sRed[w * kLLOscOut + q] = v;
+        for (int q = 0; q < kLLOscOut; q++) sAcc[w * kLLOscOut + q] = acc[q];
     }
     __syncthreads();
-    if ((int)threadIdx.x < kLLOscOut) {
-        double v = 0.0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); i++) v += sRed[i * kLLOscOut + threadIdx.x];
-        a.part_g[(size_t)e * (7 + a.n_rows) + threadIdx.x] = v;
-    }
+    // fixed-order sums of each energy's items: the layers of a row, then the rows
+    if (live)
+        for (int t = w; t < 3 * kLLOscOut; t += per) {
+            const int q = t % kLLOscOut, rr = t / kLLOscOut;
+            double v = 0.0;
+            for (int i = 0; i < nl; i++) v += sAcc[(rr * nl + i) * kLLOscOut + q];
+            sRow[rr * kLLOscOut + q] = v;
+        }
+    __syncthreads();
+    if (live)
+        for (int t = w; t < kLLOscOut; t += per)
+            a.part_g[(size_t)e * (7 + a.n_rows) + t] = (sRow[t] + sRow[kLLOscOut + t]) + sRow[2 * kLLOscOut + t];
 }
 
-// Warp w sums output slot q = w, w + nwarps, ... over energies: lanes stride
-// the energies, then a butterfly; the order is fixed, the sum deterministic.
-__global__ void __launch_bounds__(256) ll_sum_kernel(LLArgs a) {
-    const int np1 = 7 + a.n_rows;
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int q = w; q < np1; q += nw) {
-        double v = 0.0;
-        for (int e = lane; e < a.n_en; e += 32) v += a.part_g[(size_t)e * np1 + q];
-        v = warp_sum(v);
-        if (lane == 0) a.out[q] = v;
-    }
+// Block q sums output slot q over the energies: threads stride the energies,
+// then warp butterflies and the warps in order; the order is fixed, the sum
+// deterministic.  One slot per block spreads the FP64 adds over the SMs.
+__global__ void __launch_bounds__(128) ll_sum_kernel(LLArgs a) {
+    __shared__ double s_w[4];
+    const int np1 = 7 + a.n_rows, q = blockIdx.x;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double v = 0.0;
+    for (int e = threadIdx.x; e < a.n_en; e += 128) v += a.part_g[(size_t)e * np1 + q];
+    v = warp_sum(v);
+    if (lane == 0) s_w[w] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) a.out[q] = ((s_w[0] + s_w[1]) + s_w[2]) + s_w[3];
 }
 
 }  // namespace cp3
@@ -831,18 +904,20 @@ struct cp3_loglik {
     cudaStream_t stream = nullptr;
     // device
     double *d_en = nullptr, *d_cos = nullptr, *d_radii = nullptr, *d_fe = nullptr, *d_fm = nullptr, *d_counts = nullptr;
-    double *d_tab = nullptr, *d_pe = nullptr, *d_len = nullptr, *d_pl = nullptr, *d_pee = nullptr, *d_out = nullptr;
+    double *d_tab = nullptr, *d_pe = nullptr, *d_len = nullptr, *d_pl = nullptr, *d_pee = nullptr;
     double* d_pg = nullptr;
     float *d_plf = nullptr, *d_peef = nullptr, *d_fef = nullptr, *d_fmf = nullptr, *d_cntf = nullptr;
     double* d_eig = nullptr;
     float *d_tabf = nullptr, *d_pef = nullptr;
     float2* d_lenf = nullptr;
-    double *d_rhoye = nullptr, *d_yel = nullptr;
+    double* d_yel = nullptr;
     int *d_maxl = nullptr, *d_row = nullptr;
     cp3::OscParams* d_osc = nullptr;
-    // pinned staging: [OscParams][rhoye nl] up, [out] down
+    // pinned staging [OscParams, cmat][rhoye], uploaded by one copy into d_osc;
+    // h_out is mapped: ll_sum_kernel writes the results there directly
     unsigned char* h_up = nullptr;
     double* h_out = nullptr;
+    double* dh_out = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int graph_type = -1;
@@ -856,12 +931,12 @@ void ll_free(cp3_loglik* L) {
     L->exec = nullptr;
     L->graph = nullptr;
     void* ptrs[] = {L->d_en, L->d_cos, L->d_radii, L->d_fe, L->d_fm, L->d_counts, L->d_tab, L->d_pe, L->d_len,
-                    L->d_pl, L->d_pee, L->d_out, L->d_pg, L->d_rhoye, L->d_yel, L->d_maxl, L->d_row, L->d_osc,
+                    L->d_pl, L->d_pee, L->d_pg, L->d_yel, L->d_maxl, L->d_row, L->d_osc,
                     L->d_eig, L->d_tabf, L->d_pef, L->d_lenf, L->d_plf, L->d_peef, L->d_fef, L->d_fmf, L->d_cntf};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     L->d_en = L->d_cos = L->d_radii = L->d_fe = L->d_fm = L->d_counts = nullptr;
-    L->d_tab = L->d_pe = L->d_len = L->d_pl = L->d_pee = L->d_out = L->d_pg = L->d_rhoye = L->d_yel = nullptr;
+    L->d_tab = L->d_pe = L->d_len = L->d_pl = L->d_pee = L->d_pg = L->d_yel = nullptr;
     L->d_eig = nullptr;
     L->d_tabf = L->d_pef = nullptr;
     L->d_lenf = nullptr;
@@ -870,7 +945,12 @@ void ll_free(cp3_loglik* L) {
     L->d_osc = nullptr;
 }
 
-size_t up_bytes(const cp3_loglik*) { return sizeof(cp3::OscParams) + sizeof(double) * (cp3::kMaxRows + 1); }
+// Parameter block uploaded by the graph's first copy: OscParams, then the four
+// 3x3 derivative matrices of the vacuum Hamiltonian at kCmatOff.
+constexpr size_t kCmatOff = (sizeof(cp3::OscParams) + 15) / 16 * 16;
+constexpr size_t kOscBlock = kCmatOff + 36 * sizeof(double);
+
+constexpr size_t kUpBytes = kOscBlock + sizeof(double) * (cp3::kMaxRows + 1);
 
 template <class T>
 cudaError_t dmalloc_copy(T** d, const T* h, size_t n) {
@@ -882,7 +962,8 @@ cudaError_t dmalloc_copy(T** d, const T* h, size_t n) {
 cp3::LLArgs ll_args(cp3_loglik* L, int type) {
     cp3::LLArgs a{};
     a.osc = L->d_osc;
-    a.rhoye = L->d_rhoye;
+    a.cmat = (const double*)((const unsigned char*)L->d_osc + kCmatOff);
+    a.rhoye = (const double*)((const unsigned char*)L->d_osc + kOscBlock);
     a.energies = L->d_en;
     a.cosines = L->d_cos;
     a.maxl = L->d_maxl;
@@ -915,7 +996,7 @@ cp3::LLArgs ll_args(cp3_loglik* L, int type) {
     a.flux_mu_f = L->d_fmf;
     a.counts_f = L->d_cntf;
     a.norm_f = (float)L->norm;
-    a.out = L->d_out;
+    a.out = L->dh_out;
     a.layer_row = L->d_row;
     a.n_rows = L->n_rows;
     a.ye_layer = L->d_yel;
@@ -951,9 +1032,8 @@ int ll_setup(cp3_loglik* L, int type) {
     const size_t pee = (size_t)L->n_cchunk * L->n_en * cp3::kLLPerE;
     if ((e = cudaMalloc(&L->d_tab, tab * 8)) || (e = cudaMalloc(&L->d_pe, pe * 8)) || (e = cudaMalloc(&L->d_len, len * 8)) ||
         (e = cudaMalloc(&L->d_pl, pl * 8)) || (e = cudaMalloc(&L->d_pee, pee * 8)) ||
-        (e = cudaMalloc(&L->d_out, (cp3::kLLMaxParams + 1) * 8)) ||
-        (e = cudaMalloc(&L->d_pg, (size_t)L->n_en * (cp3::kLLMaxParams + 1) * 8)) || (e = cudaMalloc(&L->d_rhoye, (cp3::kMaxRows + 1) * 8)) ||
-        (e = cudaMalloc((void**)&L->d_osc, sizeof(cp3::OscParams))) ||
+        (e = cudaMalloc(&L->d_pg, (size_t)L->n_en * (cp3::kLLMaxParams + 1) * 8)) ||
+        (e = cudaMalloc((void**)&L->d_osc, kUpBytes)) ||
         (e = cudaMalloc(&L->d_eig, (size_t)L->n_en_pad * L->nl * cp3::kLLEigWords * 8)))
         return lcuda(e, "cudaMalloc(loglik)");
     if (L->mixed) {
@@ -973,9 +1053,7 @@ int ll_setup(cp3_loglik* L, int type) {
     if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking))) return lcuda(e, "cudaStreamCreate");
     e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     const cp3::LLArgs a = ll_args(L, type);
-    if (!e) e = cudaMemcpyAsync(L->d_osc, L->h_up, sizeof(cp3::OscParams), cudaMemcpyHostToDevice, cs);
-    if (!e)
-        e = cudaMemcpyAsync(L->d_rhoye, L->h_up + sizeof(cp3::OscParams), sizeof(double) * L->nl, cudaMemcpyHostToDevice, cs);
+    if (!e) e = cudaMemcpyAsync(L->d_osc, L->h_up, kOscBlock + sizeof(double) * L->nl, cudaMemcpyHostToDevice, cs);
     if (!e) {
         // energies per prep block: enough blocks to spread the FP64
         // eigen-solves over the GPU (about two per SM), at most 256 threads
@@ -996,16 +1074,27 @@ int ll_setup(cp3_loglik* L, int type) {
         e = cudaGetLastError();
     }
     if (!e) {
-        const int threads = 3 * cp3::ll_layer_lanes(L->nl);
-        const size_t smem = ((size_t)L->nl * (9 + 9 + 2 + 3 + 9) + cp3::kLLPerE + (size_t)(threads / 32) * 7) * 8;
-        cp3::ll_layer_kernel<<<L->n_en, threads, smem, cs>>>(a);
+        // energies per block: the fewest warps on the busiest SM (the
+        // kernel is bound by the FP64 issue of that SM), at most 288 threads
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, L->device);
+        sms = std::max(sms, 1);
+        int epb = 1;
+        long best = -1;
+        for (int k = 1; k <= std::max(1, 288 / (3 * L->nl)); k++) {
+            const long blocks = (L->n_en + k - 1) / k;
+            const long cost = (blocks + sms - 1) / sms * (cp3::ll_layer_threads(L->nl, k) / 32);
+            if (best < 0 || cost < best) best = cost, epb = k;
+        }
+        const int threads = cp3::ll_layer_threads(L->nl, epb);
+        const size_t smem = (size_t)epb * cp3::ll_layer_slot_doubles(L->nl) * 8;
+        cp3::ll_layer_kernel<<<(L->n_en + epb - 1) / epb, threads, smem, cs>>>(a, epb);
         e = cudaGetLastError();
     }
     if (!e) {
-        cp3::ll_sum_kernel<<<1, 256, 0, cs>>>(a);
+        cp3::ll_sum_kernel<<<7 + L->n_rows, 128, 0, cs>>>(a);
         e = cudaGetLastError();
     }
-    if (!e) e = cudaMemcpyAsync(L->h_out, L->d_out, sizeof(double) * (7 + L->n_rows), cudaMemcpyDeviceToHost, cs);
     cudaGraph_t g = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(cs, &g);
     cudaStreamDestroy(cs);
@@ -1041,8 +1130,9 @@ int cp3_loglik_create(cp3_loglik** out, int device_id, int precision, int n_cos,
     L->maxl.assign(n_cos, 0);
     cudaError_t e;
     if ((e = cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking)) ||
-        (e = cudaMallocHost((void**)&L->h_up, up_bytes(L))) ||
-        (e = cudaMallocHost((void**)&L->h_out, sizeof(double) * (cp3::kLLMaxParams + 1)))) {
+        (e = cudaMallocHost((void**)&L->h_up, kUpBytes)) ||
+        (e = cudaHostAlloc((void**)&L->h_out, sizeof(double) * (cp3::kLLMaxParams + 1), cudaHostAllocMapped)) ||
+        (e = cudaHostGetDevicePointer((void**)&L->dh_out, L->h_out, 0))) {
         int rc = lcuda(e, "loglik create");
         cp3_loglik_destroy(L);
         return rc;
@@ -1171,9 +1261,29 @@ int cp3_loglik_evaluate(cp3_loglik* L, int type, const double* params, const dou
         o.sd = std::sin(params[3]);
         o.cd = std::cos(params[3]);
         o.anti = type == CP3_ANTINEUTRINO;
+        // dH/dp of H = O diag(0, d1, d2) O^T (d1 = dm21, d2 = dm21 + dm32):
+        // theta_ij through O (dO D O^T + O D dO^T), the splittings through
+        // the outer products of O's columns
+        const double dO12[9] = {-c13 * s12, c13 * c12, 0.0, -c12, -s12, 0.0, s13 * s12, -s13 * c12, 0.0};
+        const double dO13[9] = {-s13 * c12, -s13 * s12, c13, 0.0, 0.0, 0.0, -c13 * c12, -c13 * s12, -s13};
+        const double dd[3] = {0.0, o.d1, o.d2};
+        double* C = (double*)(L->h_up + kCmatOff);
+        for (int r = 0; r < 3; r++)
+            for (int q = 0; q < 3; q++) {
+                double t12 = 0.0, t13 = 0.0;
+                for (int k = 1; k < 3; k++) {
+                    t12 += dd[k] * (dO12[3 * r + k] * O[3 * q + k] + O[3 * r + k] * dO12[3 * q + k]);
+                    t13 += dd[k] * (dO13[3 * r + k] * O[3 * q + k] + O[3 * r + k] * dO13[3 * q + k]);
+                }
+                const double a1 = O[3 * r + 1] * O[3 * q + 1], a2 = O[3 * r + 2] * O[3 * q + 2];
+                C[3 * r + q] = t12;
+                C[9 + 3 * r + q] = t13;
+                C[18 + 3 * r + q] = a1 + a2;
+                C[27 + 3 * r + q] = a2;
+            }
     }
     std::memcpy(L->h_up, &o, sizeof o);
-    double* rhoye = (double*)(L->h_up + sizeof(cp3::OscParams));
+    double* rhoye = (double*)(L->h_up + kOscBlock);
     rhoye[0] = 0.0;
     for (int l = 1; l < L->nl; l++) rhoye[l] = rhos[L->layer_row[l]] * L->ye[l - 1];
     cudaError_t e = cudaGraphLaunch(L->exec, L->stream);
