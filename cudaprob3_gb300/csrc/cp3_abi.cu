@@ -595,29 +595,7 @@ int calc_async(cp3_propagator* p, int type, bool rates) {
     pa.pb.rhoye = p->d_rhoye.p;
     pa.pb.height_cm = p->height_cm;
     // propagator.hpp:226-248 (degeneracy break) and 191-221 (mixing matrix)
-    {
-        double mv[3] = {0.0, p->dm12, p->dm12 + p->dm23};
-        const double delta = 5.0e-9;
-        if (p->dm12 == 0.0) mv[0] -= delta;
-        if (p->dm23 == 0.0) mv[2] += delta;
-        cp3::OscParams& o = pa.osc;
-        o.dm01 = mv[0] - mv[1];
-        o.dm02 = mv[0] - mv[2];
-        o.d1 = -o.dm01;
-        o.d2 = -o.dm02;
-        const double s12 = std::sin(p->th12), c12 = std::cos(p->th12);
-        const double s13 = std::sin(p->th13), c13 = std::cos(p->th13);
-        o.u00 = (c12 * c13) * (c12 * c13);
-        o.u01 = (s12 * c13) * (s12 * c13);
-        o.u02 = s13 * s13;
-        const double O[9] = {c13 * c12, c13 * s12, s13, -s12, c12, 0.0, -s13 * c12, -s13 * s12, c13};
-        std::memcpy(o.o, O, sizeof O);
-        o.s23 = std::sin(p->th23);
-        o.c23 = std::cos(p->th23);
-        o.sd = std::sin(p->dcp);
-        o.cd = std::cos(p->dcp);
-        o.anti = (type == CP3_ANTINEUTRINO) ? 1 : 0;
-    }
+    cp3::fill_osc_params(pa.osc, p->th12, p->th13, p->th23, p->dcp, p->dm12, p->dm23, type == CP3_ANTINEUTRINO);
     pa.tab = p->d_tab.p;
     pa.pe = p->d_pe.p;
     pa.len = p->d_len.p;

@@ -79,12 +79,14 @@ __global__ void __launch_bounds__(256) batch_prep_kernel(BatchPrepArgs a) {
         const int bi = blockIdx.x - a.n_eblk;
         const int2 b = a.cblk[bi];
         const BatchGrid& gr = a.grids[b.x];
-        const int c = b.y + threadIdx.y * blockDim.x + threadIdx.x;
+        // one thread per (cosine, layer): b.y is the block's first flat index
+        const int f = b.y + threadIdx.y * blockDim.x + threadIdx.x;
+        const int c = f / a.nl_pad, l = f % a.nl_pad;
         if (c >= gr.n_cos) return;
         const size_t word = MIXED ? 4 : 8;
         const GridTables g{(unsigned char*)a.tab + gr.tab_off * word, (unsigned char*)a.pe + gr.pe_off * word,
                            (unsigned char*)a.len + gr.len_off * 8, gr.n_en_pad, a.te, nl, a.nl_pad};
-        prep_cosine<MIXED>(a.cosines[gr.cos_off + c], a.maxl[gr.cos_off + c], a.radii, a.height_cm, c, g);
+        prep_cosine_layer<MIXED>(a.cosines[gr.cos_off + c], a.maxl[gr.cos_off + c], a.radii, a.height_cm, c, l, g);
     }
 }
 
@@ -373,7 +375,7 @@ int build_layout(cp3_batch* b) {
         len += (long long)g.n_cos * b->nl_pad;
         if (g.n_cos == 0 || g.n_en == 0) continue;
         for (int e0 = 0; e0 < g.n_en_pad; e0 += b->eb) b->eblk.push_back(make_int2(s, e0));
-        for (int c0 = 0; c0 < g.n_cos; c0 += cthreads) b->cblk.push_back(make_int2(s, c0));
+        for (int f0 = 0; f0 < g.n_cos * b->nl_pad; f0 += cthreads) b->cblk.push_back(make_int2(s, f0));
         for (int t = 0; t < g.n_en_pad / b->te; t++)
             for (int c0 = 0; c0 < g.n_cos; c0 += b->cchunk) {
                 const int ncl = std::min(b->cchunk, g.n_cos - c0);
@@ -426,25 +428,7 @@ int upload_descriptors(cp3_batch* b) {
     std::vector<double> rhoye((size_t)b->n_sets * b->nl);
     for (int s = 0; s < b->n_sets; s++) {
         const double* q = &b->params[6 * s];
-        cp3::OscParams& o = b->grids[s].osc;
-        double mv[3] = {0.0, q[4], q[4] + q[5]};
-        if (q[4] == 0.0) mv[0] -= 5.0e-9;
-        if (q[5] == 0.0) mv[2] += 5.0e-9;
-        o.dm01 = mv[0] - mv[1];
-        o.dm02 = mv[0] - mv[2];
-        o.d1 = -o.dm01;
-        o.d2 = -o.dm02;
-        const double s12 = std::sin(q[0]), c12 = std::cos(q[0]), s13 = std::sin(q[1]), c13 = std::cos(q[1]);
-        o.u00 = (c12 * c13) * (c12 * c13);
-        o.u01 = (s12 * c13) * (s12 * c13);
-        o.u02 = s13 * s13;
-        const double O[9] = {c13 * c12, c13 * s12, s13, -s12, c12, 0.0, -s13 * c12, -s13 * s12, c13};
-        std::memcpy(o.o, O, sizeof O);
-        o.s23 = std::sin(q[2]);
-        o.c23 = std::cos(q[2]);
-        o.sd = std::sin(q[3]);
-        o.cd = std::cos(q[3]);
-        o.anti = (b->type == CP3_ANTINEUTRINO) ? 1 : 0;
+        cp3::fill_osc_params(b->grids[s].osc, q[0], q[1], q[2], q[3], q[4], q[5], b->type == CP3_ANTINEUTRINO);
         rhoye[(size_t)s * b->nl] = 0.0;
         for (int i = 0; i < b->nl - 1; i++) rhoye[(size_t)s * b->nl + 1 + i] = b->scale[s] * b->rhos[i] * b->ye[i];
     }

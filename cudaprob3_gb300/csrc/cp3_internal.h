@@ -21,6 +21,7 @@
 // which needs about half the complex 3x3 products of the reference chain.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 
 namespace cp3 {
@@ -46,9 +47,46 @@ struct OscParams {
     double d1, d2;       // DM(1,0), DM(2,0): vacuum masses relative to m1
     double u00, u01, u02;  // |U(0,j)|^2 as the reference forms them
     double o[9];         // O = R13 R12, row-major
+    double hv[6];        // O diag(0, d1, d2) O^T: H00, H01, H02, H11, H12, H22
+    double ca, cb0, cb1, cg;  // cubic coefficients a = fac + ca, b = cb0 + fac cb1, g = fac cg
     double s23, c23, sd, cd;
     int anti;            // 1 for antineutrinos: sign of the matter term flips
 };
+
+// OscParams from the six parameters (mixing angles and dcp in radians,
+// dm21 = m2^2 - m1^2 and dm32 = m3^2 - m2^2 in eV^2): the degeneracy break of
+// propagator.hpp:226-248 and the mixing matrix of propagator.hpp:191-221.
+inline void fill_osc_params(OscParams& o, double th12, double th13, double th23, double dcp, double dm21, double dm32,
+                            bool anti) {
+    double mv[3] = {0.0, dm21, dm21 + dm32};
+    if (dm21 == 0.0) mv[0] -= 5.0e-9;
+    if (dm32 == 0.0) mv[2] += 5.0e-9;
+    o.dm01 = mv[0] - mv[1];
+    o.dm02 = mv[0] - mv[2];
+    o.d1 = -o.dm01;
+    o.d2 = -o.dm02;
+    const double s12 = std::sin(th12), c12 = std::cos(th12);
+    const double s13 = std::sin(th13), c13 = std::cos(th13);
+    o.u00 = (c12 * c13) * (c12 * c13);
+    o.u01 = (s12 * c13) * (s12 * c13);
+    o.u02 = s13 * s13;
+    const double O[9] = {c13 * c12, c13 * s12, s13, -s12, c12, 0.0, -s13 * c12, -s13 * s12, c13};
+    for (int k = 0; k < 9; k++) o.o[k] = O[k];
+    const int ij[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
+    for (int k = 0; k < 6; k++) {
+        const int i = ij[k][0], j = ij[k][1];
+        o.hv[k] = std::fma(o.d1 * O[3 * i + 1], O[3 * j + 1], (o.d2 * O[3 * i + 2]) * O[3 * j + 2]);
+    }
+    o.ca = o.dm01 + o.dm02;
+    o.cb0 = o.dm01 * o.dm02;
+    o.cb1 = o.dm01 * (1.0 - o.u01) + o.dm02 * (1.0 - o.u02);
+    o.cg = o.dm01 * o.dm02 * o.u00;
+    o.s23 = std::sin(th23);
+    o.c23 = std::cos(th23);
+    o.sd = std::sin(dcp);
+    o.cd = std::cos(dcp);
+    o.anti = anti ? 1 : 0;
+}
 
 // One problem for the kernels (device pointers).
 struct Problem {

@@ -49,19 +49,22 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a) {
         __syncthreads();
         if (live) prep_overlap<MIXED>(l, e, g, vme);
     } else {
-        const int c = (blockIdx.x - a.n_energy_blocks) * (blockDim.x * blockDim.y) + threadIdx.y * blockDim.x +
-                      threadIdx.x;
+        // one thread per (cosine, layer)
+        const long long f = (long long)(blockIdx.x - a.n_energy_blocks) * (blockDim.x * blockDim.y) +
+                            threadIdx.y * blockDim.x + threadIdx.x;
+        const int c = (int)(f / a.pb.nl_pad), l = (int)(f % a.pb.nl_pad);
         if (c >= a.pb.n_cos) return;
         const double cz = a.pb.cosines[c];
         const int M = a.pb.maxlayers[c];
-        prep_cosine<MIXED>(cz, M, a.pb.radii, a.pb.height_cm, c, g);
-        // atmosphere segment at every production height (physics.hpp:613-616, 561-562)
-        for (int h = 0; h < a.n_h; h++) {
+        prep_cosine_layer<MIXED>(cz, M, a.pb.radii, a.pb.height_cm, c, l, g);
+        // atmosphere segment at every production height (physics.hpp:613-616,
+        // 561-562), spread over the cosine's layer threads
+        for (int h = l; h < a.n_h; h += a.pb.nl_pad) {
             const double L0 = layer_length_km(a.pb.radii, 0, M, cz, path_length_cm(cz, a.heights_cm[h]));
             const size_t idx = (size_t)c * a.n_h + h;
             if (MIXED) {
-                const float hi = (float)L0;
-                ((float2*)a.lenh)[idx] = make_float2(hi, (float)(L0 - (double)hi));
+                const float hi = f32_rn(L0);
+                ((float2*)a.lenh)[idx] = make_float2(hi, f32_rn(L0 - f64_of(hi)));
             } else {
                 ((double*)a.lenh)[idx] = L0;
             }
@@ -125,7 +128,7 @@ cudaError_t launch_prep(bool mixed, PrepArgs a, cudaStream_t s) {
     const int eb = std::max(1, 256 / nl);
     a.n_energy_blocks = (a.pb.n_en_pad + eb - 1) / eb;
     const int threads = nl * eb;
-    const int nbC = (a.pb.n_cos + threads - 1) / threads;
+    const long long nbC = ((long long)a.pb.n_cos * a.pb.nl_pad + threads - 1) / threads;
     const size_t smem = (size_t)eb * nl * 9 * sizeof(double);
     if (a.n_energy_blocks + nbC == 0) return cudaSuccess;
     dim3 block(nl, eb);

@@ -171,29 +171,30 @@ __global__ void __launch_bounds__(256) ll_prep_kernel(LLArgs a) {
                 const double* t = a.tab + ((size_t)tile * nl + l) * kFp64Words * kLLTile + ln;
                 float* f = a.tabf + ((size_t)tile * nl + l) * kLLFWords * kLLTile + ln;
 #pragma unroll
-                for (int q = 0; q < 9; q++) f[q * kLLTile] = (float)t[q * kLLTile];
+                for (int q = 0; q < 9; q++) f[q * kLLTile] = f32_rn(t[q * kLLTile]);
 #pragma unroll
                 for (int k = 0; k < 2; k++) {
                     const double kd = t[(9 + k) * kLLTile];
-                    const float kh = (float)kd;
+                    const float kh = f32_rn(kd);
                     f[(9 + 2 * k) * kLLTile] = kh;
-                    f[(10 + 2 * k) * kLLTile] = (float)(kd - (double)kh);
+                    f[(10 + 2 * k) * kLLTile] = f32_rn(kd - f64_of(kh));
                 }
-                if (l == 0)
-                    for (int w = 0; w < 18; w++)
-                        a.pef[(size_t)w * a.n_en_pad + e] = (float)a.pe[(size_t)w * a.n_en_pad + e];
+                // the energy's 18 words, spread over its layers' threads
+                for (int w = l; w < 18; w += nl)
+                    a.pef[(size_t)w * a.n_en_pad + e] = f32_rn(a.pe[(size_t)w * a.n_en_pad + e]);
             }
         }
     } else {
-        const int c = (blockIdx.x - nbE) * (blockDim.x * blockDim.y) + threadIdx.y * blockDim.x + threadIdx.x;
+        // one thread per (cosine, layer)
+        const int f = (blockIdx.x - nbE) * (blockDim.x * blockDim.y) + threadIdx.y * blockDim.x + threadIdx.x;
+        const int c = f / a.nl_pad, l = f % a.nl_pad;
         if (c >= a.n_cos) return;
-        prep_cosine<false>(a.cosines[c], a.maxl[c], a.radii, a.height_cm, c, g);
-        if (a.lenf)
-            for (int l = 0; l < a.nl_pad; l++) {
-                const double L = a.len[(size_t)c * a.nl_pad + l];
-                const float h = (float)L;
-                a.lenf[(size_t)c * a.nl_pad + l] = make_float2(h, (float)(L - (double)h));
-            }
+        prep_cosine_layer<false>(a.cosines[c], a.maxl[c], a.radii, a.height_cm, c, l, g);
+        if (a.lenf) {
+            const double L = a.len[(size_t)c * a.nl_pad + l];
+            const float h = f32_rn(L);
+            a.lenf[(size_t)c * a.nl_pad + l] = make_float2(h, f32_rn(L - f64_of(h)));
+        }
     }
 }
 
@@ -253,7 +254,7 @@ struct LLSrc<float> {
 };
 
 template <class R>
-__global__ void __launch_bounds__(128) ll_pair_kernel(LLArgs a) {
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) ll_pair_kernel(LLArgs a) {
     using C = Cx<R>;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int e = blockIdx.x * 4 + warp;
@@ -607,7 +608,7 @@ struct FloatTwoSum {
         c += (s - (t - bp)) + (x - bp);
         s = t;
     }
-    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+    __device__ __forceinline__ double value() const { return f64_of(s) + f64_of(c); }
 };
 
 // Item (slot, r, l) of block b: energy b * epb + slot, row r in {0, 1, 2} of
@@ -1061,7 +1062,7 @@ int ll_setup(cp3_loglik* L, int type) {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, L->device);
         const int eb = std::max(1, std::min(256 / L->nl, std::max(32 / L->nl, L->n_en_pad / std::max(1, 2 * sms))));
         const int nbE = (L->n_en_pad + eb - 1) / eb;
-        const int nbC = (L->n_cos + L->nl * eb - 1) / (L->nl * eb);
+        const int nbC = (L->n_cos * L->nl_pad + L->nl * eb - 1) / (L->nl * eb);
         cp3::ll_prep_kernel<<<nbE + nbC, dim3(L->nl, eb), (size_t)eb * L->nl * 9 * 8, cs>>>(a);
         e = cudaGetLastError();
     }
@@ -1241,26 +1242,11 @@ int cp3_loglik_evaluate(cp3_loglik* L, int type, const double* params, const dou
     }
     // parameters into the pinned staging buffer (read by the graph's first copies)
     cp3::OscParams o{};
+    cp3::fill_osc_params(o, params[0], params[1], params[2], params[3], params[4], params[5], type == CP3_ANTINEUTRINO);
     {
-        double mv[3] = {0.0, params[4], params[4] + params[5]};
-        if (params[4] == 0.0) mv[0] -= 5.0e-9;
-        if (params[5] == 0.0) mv[2] += 5.0e-9;
-        o.dm01 = mv[0] - mv[1];
-        o.dm02 = mv[0] - mv[2];
-        o.d1 = -o.dm01;
-        o.d2 = -o.dm02;
         const double s12 = std::sin(params[0]), c12 = std::cos(params[0]);
         const double s13 = std::sin(params[1]), c13 = std::cos(params[1]);
-        o.u00 = (c12 * c13) * (c12 * c13);
-        o.u01 = (s12 * c13) * (s12 * c13);
-        o.u02 = s13 * s13;
-        const double O[9] = {c13 * c12, c13 * s12, s13, -s12, c12, 0.0, -s13 * c12, -s13 * s12, c13};
-        std::memcpy(o.o, O, sizeof O);
-        o.s23 = std::sin(params[2]);
-        o.c23 = std::cos(params[2]);
-        o.sd = std::sin(params[3]);
-        o.cd = std::cos(params[3]);
-        o.anti = type == CP3_ANTINEUTRINO;
+        const double* O = o.o;
         // dH/dp of H = O diag(0, d1, d2) O^T (d1 = dm21, d2 = dm21 + dm32):
         // theta_ij through O (dO D O^T + O D dO^T), the splittings through
         // the outer products of O's columns

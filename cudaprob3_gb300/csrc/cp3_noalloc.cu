@@ -190,29 +190,7 @@ extern "C" int cp3_propagate_noalloc(int precision, int type, const double* d_co
     pa.pb.radii = d_radii;
     pa.pb.rhoye = d_rhoye;
     pa.pb.height_cm = height_km * 100000.0;
-    {
-        // propagator.hpp:191-248
-        double mv[3] = {0.0, dm12sq, dm12sq + dm23sq};
-        if (dm12sq == 0.0) mv[0] -= 5.0e-9;
-        if (dm23sq == 0.0) mv[2] += 5.0e-9;
-        OscParams& o = pa.osc;
-        o.dm01 = mv[0] - mv[1];
-        o.dm02 = mv[0] - mv[2];
-        o.d1 = -o.dm01;
-        o.d2 = -o.dm02;
-        const double s12 = std::sin(theta12), c12 = std::cos(theta12);
-        const double s13 = std::sin(theta13), c13 = std::cos(theta13);
-        o.u00 = (c12 * c13) * (c12 * c13);
-        o.u01 = (s12 * c13) * (s12 * c13);
-        o.u02 = s13 * s13;
-        const double O[9] = {c13 * c12, c13 * s12, s13, -s12, c12, 0.0, -s13 * c12, -s13 * s12, c13};
-        for (int i = 0; i < 9; i++) o.o[i] = O[i];
-        o.s23 = std::sin(theta23);
-        o.c23 = std::cos(theta23);
-        o.sd = std::sin(dcp);
-        o.cd = std::cos(dcp);
-        o.anti = type == CP3_ANTINEUTRINO ? 1 : 0;
-    }
+    fill_osc_params(pa.osc, theta12, theta13, theta23, dcp, dm12sq, dm23sq, type == CP3_ANTINEUTRINO);
     pa.tab = tab;
     pa.pe = pe;
     pa.len = len;

@@ -8,6 +8,7 @@
 #pragma once
 
 #include <cmath>
+#include <cstring>
 
 #include "cp3_internal.h"
 
@@ -32,18 +33,101 @@ namespace cp3 {
 // which makes every basis right-handed (the propagation kernels rely on
 // det T_l = +1 for T_l = V_{l+1}^T V_l).
 //
-// FP64 divisions and square roots are long instruction sequences on GB300's
-// narrow FP64 pipe, so the solve avoids them where FP32 or a refinement
-// suffices: the trigonometric first guess is FP32 throughout; Newton steps
-// scale by an FP32 reciprocal of the derivative (the step error is then
-// quadratic plus 1e-7 times linear, below 1e-20 relative after two steps);
-// quotients use div_nr; normalisations use rsqrt.
+// On GB300 every warp-wide FP64 instruction holds its SM sub-partition for
+// about 64 cycles whatever the number of active lanes (measured: a dependent
+// DFMA chain, and four independent ones, cost 64 cycles per instruction; four
+// warps on one SM 76 cycles), and FP64 compares, min/max and conversions run
+// on the same pipe.  So the solve keeps off that pipe whatever FP32 or the
+// integer pipe can do exactly or well enough: the trigonometric first guess
+// and every ordering decision are FP32; Newton steps scale by an FP32
+// reciprocal of the derivative (the step error is then quadratic plus 1e-7
+// times linear, below 1e-20 relative after two steps); quotients use div_nr;
+// normalisations use rsqrt; sign and magnitude tests and the conversions to
+// Q1.30 and float read the bit patterns on the integer pipe; the branch of the
+// projector column is a select, not divergent code.
+
+// Bit pattern of a double.
+CP3_HD unsigned long long dbits(double x) {
+#ifdef __CUDA_ARCH__
+    return (unsigned long long)__double_as_longlong(x);
+#else
+    unsigned long long u;
+    std::memcpy(&u, &x, 8);
+    return u;
+#endif
+}
+// |x| as an integer key: |x| >= |y| iff abs_key(x) >= abs_key(y) (no NaNs).
+CP3_HD unsigned long long abs_key(double x) { return dbits(x) & 0x7fffffffffffffffULL; }
+CP3_HD bool sign_bit(double x) { return (long long)dbits(x) < 0; }
+CP3_HD bool nonzero(double x) { return abs_key(x) != 0; }
+// x < y (no NaNs; -0 orders below +0).
+CP3_HD bool less_than(double x, double y) {
+    const long long a = (long long)dbits(x), b = (long long)dbits(y);
+    return (a ^ ((a >> 63) & 0x7fffffffffffffffLL)) < (b ^ ((b >> 63) & 0x7fffffffffffffffLL));
+}
+
+// __double2int_rn(x * 2^30) for |x| < 2 from the bits: the significand
+// shifted right by 1045 - exponent (at most 63: anything below 2^-31 rounds to
+// zero), rounded half to even.  Branch-free.
+CP3_HD int q30_rn(double x) {
+    const unsigned long long b = dbits(x);
+    const int ex = (int)((b >> 52) & 0x7ff);
+    const int sh = (1045 - ex < 63) ? 1045 - ex : 63;
+    const unsigned long long m = (b & 0xfffffffffffffULL) | (1ULL << 52);
+    const unsigned long long r = (m + ((1ULL << (sh - 1)) - 1) + ((m >> sh) & 1)) >> sh;
+    return ((long long)b < 0) ? -(int)r : (int)r;
+}
+
+// (float)x rounded to nearest even from the bits, branch-free; results below
+// FLT_MIN flush to a signed zero (the kernels convert magnitudes far above
+// it), overflow gives infinity and NaN stays NaN.
+CP3_HD float f32_rn(double x) {
+    const unsigned long long b = dbits(x);
+    const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+    const int ex = (int)((b >> 52) & 0x7ff);
+    const unsigned long long m = b & 0xfffffffffffffULL;
+    const unsigned int r = (unsigned int)((m + 0xfffffffULL + ((m >> 29) & 1)) >> 29);  // may carry into the exponent
+    unsigned int u = (sign | ((unsigned int)(ex - 1023 + 127) << 23)) + r;
+    u = (ex < 1023 - 126) ? sign : u;
+    u = (ex > 1023 + 127) ? (sign | 0x7f800000u) : u;
+    u = (ex == 0x7ff && m != 0) ? 0x7fc00000u : u;
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(u);
+#else
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+#endif
+}
+
+// (double)f from the bits, branch-free and exact for normal floats, zero,
+// infinity and NaN; subnormal floats flush to a signed zero.
+CP3_HD double f64_of(float f) {
+#ifdef __CUDA_ARCH__
+    const unsigned int u = __float_as_uint(f);
+#else
+    unsigned int u;
+    std::memcpy(&u, &f, 4);
+#endif
+    const unsigned int ex = (u >> 23) & 0xff;
+    const unsigned int ex64 = (ex == 0xff) ? 0x7ffu : ex + (1023 - 127);
+    unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) | ((unsigned long long)ex64 << 52) |
+                           ((unsigned long long)(u & 0x7fffffu) << 29);
+    b = (ex == 0) ? ((unsigned long long)(u & 0x80000000u) << 32) : b;
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)b);
+#else
+    double d;
+    std::memcpy(&d, &b, 8);
+    return d;
+#endif
+}
 
 // a / b to about 1 ulp: FP32 reciprocal estimate refined by two Newton-Raphson
 // corrections of the quotient, q += r (a - q b) (each squares the relative
 // error: 1e-7 -> 1e-14 -> 1e-28).  |b| must lie in FP32's normal range.
 CP3_HD double div_nr(double a, double b) {
-    const double r = (double)(1.0f / (float)b);
+    const double r = f64_of(1.0f / f32_rn(b));
     double q = a * r;
     q = fma(r, fma(-q, b, a), q);
     q = fma(r, fma(-q, b, a), q);
@@ -63,138 +147,117 @@ CP3_HD double cubic_newton(double x, double a, double b, double g) {
     for (int it = 0; it < 2; it++) {
         const double p = fma(fma(x + a, x, b), x, g);
         const double dp = fma(fma(3.0, x, 2.0 * a), x, b);
-        if (dp != 0.0) x -= p * (double)(1.0f / (float)dp);
+        x = nonzero(dp) ? x - p * f64_of(1.0f / f32_rn(dp)) : x;
     }
     return x;
 }
 
 CP3_HD void eigvec_of(const double H[9], double m, double ma, double mb, double v[3]) {
     // columns of N = (H - ma)(H - mb) are parallel to the eigenvector of m;
-    // take the one with the largest diagonal entry
+    // take the one with the largest diagonal entry (H symmetric)
+    (void)m;
     const double a0 = H[0] - ma, a4 = H[4] - ma, a8 = H[8] - ma;
     const double b0 = H[0] - mb, b4 = H[4] - mb, b8 = H[8] - mb;
-    const double n00 = a0 * b0 + H[1] * H[3] + H[2] * H[6];
-    const double n11 = H[3] * H[1] + a4 * b4 + H[5] * H[7];
-    const double n22 = H[6] * H[2] + H[7] * H[5] + a8 * b8;
-    double c0, c1, c2;
-    if (fabs(n00) >= fabs(n11) && fabs(n00) >= fabs(n22)) {
-        c0 = n00;
-        c1 = H[3] * b0 + a4 * H[3] + H[5] * H[6];
-        c2 = H[6] * b0 + H[7] * H[3] + a8 * H[6];
-    } else if (fabs(n11) >= fabs(n22)) {
-        c0 = a0 * H[1] + H[1] * b4 + H[2] * H[7];
-        c1 = n11;
-        c2 = H[6] * H[1] + H[7] * b4 + a8 * H[7];
-    } else {
-        c0 = a0 * H[2] + H[1] * H[5] + H[2] * b8;
-        c1 = H[3] * H[2] + a4 * H[5] + H[5] * b8;
-        c2 = n22;
-    }
+    const double n00 = a0 * b0 + H[1] * H[1] + H[2] * H[2];
+    const double n11 = H[1] * H[1] + a4 * b4 + H[5] * H[5];
+    const double n22 = H[2] * H[2] + H[5] * H[5] + a8 * b8;
+    const unsigned long long k0 = abs_key(n00), k1 = abs_key(n11), k2 = abs_key(n22);
+    const int p = (k0 >= k1 && k0 >= k2) ? 0 : (k1 >= k2) ? 1 : 2;
+    // column p of H - mb, then c = (H - ma) x
+    const double x0 = (p == 0) ? b0 : (p == 1) ? H[1] : H[2];
+    const double x1 = (p == 1) ? b4 : (p == 0) ? H[1] : H[5];
+    const double x2 = (p == 2) ? b8 : (p == 0) ? H[2] : H[5];
+    const double c0 = a0 * x0 + H[1] * x1 + H[2] * x2;
+    const double c1 = H[1] * x0 + a4 * x1 + H[5] * x2;
+    const double c2 = H[2] * x0 + H[5] * x1 + a8 * x2;
     const double n2 = c0 * c0 + c1 * c1 + c2 * c2;
-    double inv = (n2 > 0.0) ? rsqrt_fp64(n2) : 0.0;
+    double inv = nonzero(n2) ? rsqrt_fp64(n2) : 0.0;
     // deterministic sign: largest component positive
     double big = c0;
-    if (fabs(c1) > fabs(big)) big = c1;
-    if (fabs(c2) > fabs(big)) big = c2;
-    if (big < 0.0) inv = -inv;
+    if (abs_key(c1) > abs_key(big)) big = c1;
+    if (abs_key(c2) > abs_key(big)) big = c2;
+    if (sign_bit(big)) inv = -inv;
     v[0] = c0 * inv;
     v[1] = c1 * inv;
     v[2] = c2 * inv;
 }
 
 CP3_HD void layer_eigen(const OscParams& p, double E, double rhoye, double m[3], double V[9]) {
-    // physics.hpp:277-295: matter term and the cubic's coefficients
+    // physics.hpp:277-295: matter term and the cubic's coefficients (the
+    // parameter-only products are formed once on the host)
     const double fac = p.anti ? kGF * E * rhoye : -(kGF * E * rhoye);
-    const double a = fac + p.dm01 + p.dm02;
-    const double b = p.dm01 * p.dm02 + fac * (p.dm01 * (1.0 - p.u01) + p.dm02 * (1.0 - p.u02));
-    const double g = fac * p.dm01 * p.dm02 * p.u00;
+    const double a = fac + p.ca;
+    const double b = fma(fac, p.cb1, p.cb0);
+    const double g = fac * p.cg;
     // physics.hpp:298-324: trigonometric roots as an FP32 first guess (the
     // numerator and a^2 - 3b are formed in FP64: they cancel), then Newton
     double tmp = a * a - 3.0 * b;
-    if (tmp < 0.0) tmp = 0.0;
-    const float tmpf = (float)tmp;
+    if (sign_bit(tmp)) tmp = 0.0;
+    const float tmpf = f32_rn(tmp);
     const float sqf = sqrtf(tmpf);
-    float arg = (float)(2.0 * a * a * a - 9.0 * a * b + 27.0 * g) / (2.0f * sqf * tmpf);
+    float arg = f32_rn(2.0 * a * a * a - 9.0 * a * b + 27.0 * g) / (2.0f * sqf * tmpf);
     if (!(fabsf(arg) <= 1.0f)) arg = (arg > 0.0f) ? 1.0f : -1.0f;
     const float th = acosf(arg) * (1.0f / 3.0f);
     float sf, cf;
     sincosf(th, &sf, &cf);
-    const double c = cf, s = sf;
-    const double h = 0.86602540378443864676;  // sin(2pi/3)
-    const double amp = -(2.0 / 3.0) * (double)sqf;
-    const double sh = a * (-1.0 / 3.0);
-    {
-    double q[3];
-    q[0] = amp * c + sh;                   // cos(th)
-    q[1] = amp * (-0.5 * c + h * s) + sh;  // cos(th - 2pi/3)
-    q[2] = amp * (-0.5 * c - h * s) + sh;  // cos(th + 2pi/3)
+    const float hf = 0.866025403784438647f;  // sin(2pi/3)
+    const float ampf = -(2.0f / 3.0f) * sqf;
+    const float shf = f32_rn(a) * (-1.0f / 3.0f);
+    const float q0 = ampf * cf + shf;                     // cos(th)
+    const float q1 = ampf * (-0.5f * cf + hf * sf) + shf; // cos(th - 2pi/3)
+    const float q2 = ampf * (-0.5f * cf - hf * sf) + shf; // cos(th + 2pi/3)
     // Newton converges fast only on a well separated root, and the degeneracy
     // break leaves a pair 5e-9 eV^2 apart: refine the most isolated root i,
     // then take the other two from the deflated quadratic x^2 - S x + P with
     // S = -a - m_i and P = -g/m_i (or b - m_i S when m_i is not the largest).
-    const double e0 = fmin(fabs(q[0] - q[1]), fabs(q[0] - q[2]));
-    const double e1 = fmin(fabs(q[1] - q[0]), fabs(q[1] - q[2]));
-    const double e2 = fmin(fabs(q[2] - q[0]), fabs(q[2] - q[1]));
+    const float d01 = fabsf(q0 - q1), d02 = fabsf(q0 - q2), d12 = fabsf(q1 - q2);
+    const float e0 = fminf(d01, d02), e1 = fminf(d01, d12), e2 = fminf(d02, d12);
     const int ri = (e0 >= e1 && e0 >= e2) ? 0 : (e1 >= e2) ? 1 : 2;
-    const int rj = (ri + 1) % 3, rk = (ri + 2) % 3;
-    const double qi = (ri == 0) ? q[0] : (ri == 1) ? q[1] : q[2];
-    const double qj = (rj == 0) ? q[0] : (rj == 1) ? q[1] : q[2];
-    const double qk = (rk == 0) ? q[0] : (rk == 1) ? q[1] : q[2];
-    const double mi = cubic_newton(qi, a, b, g);
+    const int rj = (ri == 2) ? 0 : ri + 1, rk = (ri == 0) ? 2 : ri - 1;
+    const float qi = (ri == 0) ? q0 : (ri == 1) ? q1 : q2;
+    const float qj = (rj == 0) ? q0 : (rj == 1) ? q1 : q2;
+    const float qk = (rk == 0) ? q0 : (rk == 1) ? q1 : q2;
+    const float ej = (rj == 0) ? e0 : (rj == 1) ? e1 : e2;
+    const float ek = (rk == 0) ? e0 : (rk == 1) ? e1 : e2;
+    const double mi = cubic_newton(f64_of(qi), a, b, g);
     const double S = -a - mi;
-    const double P = (fabs(mi) >= fabs(qj) && fabs(mi) >= fabs(qk) && mi != 0.0) ? div_nr(-g, mi) : b - mi * S;
+    const double P =
+        (fabsf(qi) >= fabsf(qj) && fabsf(qi) >= fabsf(qk) && nonzero(mi)) ? div_nr(-g, mi) : b - mi * S;
     double disc = S * S - 4.0 * P;
-    if (disc < 0.0) disc = 0.0;
+    if (sign_bit(disc)) disc = 0.0;
     const double big = 0.5 * (S + copysign(sqrt(disc), S));
-    const double small = (big != 0.0) ? div_nr(P, big) : 0.0;
-    const double hi = fmax(big, small), lo = fmin(big, small);
+    const double small = nonzero(big) ? div_nr(P, big) : 0.0;
+    const bool big_lo = less_than(big, small);
+    const double hi = big_lo ? small : big, lo = big_lo ? big : small;
     const double mj = (qj >= qk) ? hi : lo;
     const double mk = (qj >= qk) ? lo : hi;
     m[0] = (ri == 0) ? mi : (rj == 0) ? mj : mk;
     m[1] = (ri == 1) ? mi : (rj == 1) ? mj : mk;
     m[2] = (ri == 2) ? mi : (rj == 2) ? mj : mk;
-    }
 
     // H_r = O diag(0, d1, d2) O^T - fac e0 e0^T
-    double H[9];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++)
-            H[3 * i + j] = p.d1 * p.o[3 * i + 1] * p.o[3 * j + 1] + p.d2 * p.o[3 * i + 2] * p.o[3 * j + 2];
-    H[0] -= fac;
+    const double H[9] = {p.hv[0] - fac, p.hv[1], p.hv[2], p.hv[1], p.hv[3], p.hv[4], p.hv[2], p.hv[4], p.hv[5]};
 
     // The most isolated eigenvalue i gets its projector column; the next most
     // isolated j too, made exactly orthogonal to v_i; the third is their cross
     // product.  A near-degenerate pair (the degeneracy break of
-    // propagator.hpp:226-248) then still yields an orthonormal basis.
-    const double g0 = fmin(fabs(m[0] - m[1]), fabs(m[0] - m[2]));
-    const double g1 = fmin(fabs(m[1] - m[0]), fabs(m[1] - m[2]));
-    const double g2 = fmin(fabs(m[2] - m[0]), fabs(m[2] - m[1]));
-    int i = 0;
-    if (g1 > g0) i = 1;
-    if (g2 > (i == 0 ? g0 : g1)) i = 2;
-    const int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
-    const double gi1 = (i1 == 0) ? g0 : (i1 == 1) ? g1 : g2;
-    const double gi2 = (i2 == 0) ? g0 : (i2 == 1) ? g1 : g2;
-    const bool cyc = gi1 >= gi2;  // j = i+1, k = i+2 (cyclic) or j = i+2, k = i+1
-    const int j = cyc ? i1 : i2;
-    const double mi = (i == 0) ? m[0] : (i == 1) ? m[1] : m[2];
-    const double mj = (j == 0) ? m[0] : (j == 1) ? m[1] : m[2];
-    const int k = 3 - i - j;
-    const double mk = (k == 0) ? m[0] : (k == 1) ? m[1] : m[2];
+    // propagator.hpp:226-248) then still yields an orthonormal basis.  The
+    // ranking is the FP32 one of the first guesses.
+    const bool cyc = ej >= ek;  // j = i+1, k = i+2 (cyclic) or j = i+2, k = i+1
+    const int i = ri, j = cyc ? rj : rk;
+    const double mje = cyc ? mj : mk, mke = cyc ? mk : mj;
     double vi[3], vj[3], vk[3];
-    eigvec_of(H, mi, mj, mk, vi);
-    eigvec_of(H, mj, mk, mi, vj);
+    eigvec_of(H, mi, mje, mke, vi);
+    eigvec_of(H, mje, mke, mi, vj);
     const double d = vj[0] * vi[0] + vj[1] * vi[1] + vj[2] * vi[2];
     vj[0] -= d * vi[0];
     vj[1] -= d * vi[1];
     vj[2] -= d * vi[2];
     const double nj2 = vj[0] * vj[0] + vj[1] * vj[1] + vj[2] * vj[2];
-    const double rj = (nj2 > 0.0) ? rsqrt_fp64(nj2) : 0.0;
-    vj[0] *= rj;
-    vj[1] *= rj;
-    vj[2] *= rj;
+    const double rj2 = nonzero(nj2) ? rsqrt_fp64(nj2) : 0.0;
+    vj[0] *= rj2;
+    vj[1] *= rj2;
+    vj[2] *= rj2;
     // (i, j, k) cyclic: v_k = v_i x v_j; otherwise v_k = v_j x v_i
     const double sgn = cyc ? 1.0 : -1.0;
     vk[0] = sgn * (vi[1] * vj[2] - vi[2] * vj[1]);
@@ -211,7 +274,7 @@ CP3_HD void layer_eigen(const OscParams& p, double E, double rhoye, double m[3],
 // eigenvalue 0 is -LoEfac * (m_k - m_0) * L / E (physics.hpp:461-467) with the
 // per-layer common phase of m_0 removed; in turns per km that is
 // phase_rate_factor(E) * (m_k - m_0), the factor computed once per (energy, layer).
-CP3_HD double phase_rate_factor(double E) { return -kLoEfac / (kTwoPi * E); }
+CP3_HD double phase_rate_factor(double E) { return div_nr(-kLoEfac / kTwoPi, E); }
 
 // Total path length including the production height (physics.hpp:615-616), cm.
 CP3_HD double path_length_cm(double c, double height_cm) {
@@ -222,10 +285,17 @@ CP3_HD double path_length_cm(double c, double height_cm) {
 // Length in km of the segment of layer `l` (0 = atmosphere, 1..M shells from
 // the outside in) crossed by a trajectory of cosine c that reaches shell M:
 // physics.hpp:555-580 evaluated for the inbound half, l <= M.
+// x / 1e5 (cm to km): the product with the rounded reciprocal and one FMA
+// correction from the exact remainder, instead of an FP64 division.
+CP3_HD double km_of_cm(double x) {
+    const double q = x * 1.0e-5;
+    return fma(fma(-q, kKm2Cm, x), 1.0e-5, q);
+}
+
 CP3_HD double layer_length_km(const double* radii, int l, int M, double c, double path_cm) {
-    if (c >= 0.0) return path_cm / kKm2Cm;
+    if (c >= 0.0) return km_of_cm(path_cm);
     const double earth_cm = -2.0 * c * (kREarth * kKm2Cm);
-    if (l == 0) return (path_cm - earth_cm) / kKm2Cm;
+    if (l == 0) return km_of_cm(path_cm - earth_cm);
     const int i = l - 1;
     const double perp2 = kREarth * kREarth * (1.0 - c * c);
     double q = radii[i] * radii[i] - perp2;
@@ -233,9 +303,9 @@ CP3_HD double layer_length_km(const double* radii, int l, int M, double c, doubl
     if (i < M - 1) {
         double qn = radii[i + 1] * radii[i + 1] - perp2;
         const double cross_next = 2.0 * sqrt(qn > 0.0 ? qn : 0.0);
-        return (0.5 * (cross_this - cross_next) * kKm2Cm) / kKm2Cm;
+        return km_of_cm(0.5 * (cross_this - cross_next) * kKm2Cm);
     }
-    return (cross_this * kKm2Cm) / kKm2Cm;
+    return km_of_cm(cross_this * kKm2Cm);
 }
 
 }  // namespace cp3

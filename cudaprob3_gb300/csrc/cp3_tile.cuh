@@ -47,11 +47,11 @@ __device__ __forceinline__ void prep_energy_layer(const OscParams& osc, double E
     const size_t base = ((size_t)tile * g.nl + l) * W * te + lane;
     if (MIXED) {
         int* t = (int*)g.tab;
-        const float k1h = (float)k1, k2h = (float)k2;
+        const float k1h = f32_rn(k1), k2h = f32_rn(k2);
         t[base + 9 * (size_t)te] = __float_as_int(k1h);
-        t[base + 10 * (size_t)te] = __float_as_int((float)(k1 - (double)k1h));
+        t[base + 10 * (size_t)te] = __float_as_int(f32_rn(k1 - f64_of(k1h)));
         t[base + 11 * (size_t)te] = __float_as_int(k2h);
-        t[base + 12 * (size_t)te] = __float_as_int((float)(k2 - (double)k2h));
+        t[base + 12 * (size_t)te] = __float_as_int(f32_rn(k2 - f64_of(k2h)));
     } else {
         double* t = (double*)g.tab;
         t[base + 9 * (size_t)te] = k1;
@@ -71,7 +71,7 @@ __device__ __forceinline__ void prep_energy_layer(const OscParams& osc, double E
         for (int q = 0; q < 9; q++) {
             const size_t idx = (size_t)(off + q) * g.n_en_pad + e;
             if (MIXED)
-                ((int*)g.pe)[idx] = __double2int_rn(w[q] * 1073741824.0);
+                ((int*)g.pe)[idx] = q30_rn(w[q]);
             else
                 ((double*)g.pe)[idx] = w[q];
         }
@@ -91,26 +91,25 @@ __device__ __forceinline__ void prep_overlap(int l, int e, const GridTables& g, 
             const double tij = (l + 1 < g.nl) ? vn[i] * vme[j] + vn[3 + i] * vme[3 + j] + vn[6 + i] * vme[6 + j]
                                               : (i == j ? 1.0 : 0.0);
             if (MIXED)
-                ((int*)g.tab)[base + (size_t)(3 * i + j) * te] = __double2int_rn(tij * 1073741824.0);
+                ((int*)g.tab)[base + (size_t)(3 * i + j) * te] = q30_rn(tij);
             else
                 ((double*)g.tab)[base + (size_t)(3 * i + j) * te] = tij;
         }
 }
 
-// Segment lengths of trajectory c (layers 0..M, zero beyond).
+// Segment length of layer l of trajectory c (zero beyond M).  One thread per
+// (cosine, layer): a thread running all layers in sequence would be a chain
+// of some 25 FP64 square roots, far longer than any eigen-solve.
 template <bool MIXED>
-__device__ __forceinline__ void prep_cosine(double cz, int M, const double* radii, double height_cm, int c,
-                                            const GridTables& g) {
-    const double path = path_length_cm(cz, height_cm);
-    for (int l = 0; l < g.nl_pad; l++) {
-        const double L = (l <= M) ? layer_length_km(radii, l, M, cz, path) : 0.0;
-        const size_t idx = (size_t)c * g.nl_pad + l;
-        if (MIXED) {
-            const float h = (float)L;
-            ((float2*)g.len)[idx] = make_float2(h, (float)(L - (double)h));
-        } else {
-            ((double*)g.len)[idx] = L;
-        }
+__device__ __forceinline__ void prep_cosine_layer(double cz, int M, const double* radii, double height_cm, int c,
+                                                  int l, const GridTables& g) {
+    const double L = (l <= M) ? layer_length_km(radii, l, M, cz, path_length_cm(cz, height_cm)) : 0.0;
+    const size_t idx = (size_t)c * g.nl_pad + l;
+    if (MIXED) {
+        const float h = f32_rn(L);
+        ((float2*)g.len)[idx] = make_float2(h, f32_rn(L - f64_of(h)));
+    } else {
+        ((double*)g.len)[idx] = L;
     }
 }
 
