@@ -203,6 +203,9 @@ struct TurnSum {
 };
 
 // ------------------------------------------------------------------ FP64 ----
+// max(x, 0) for a double on the integer pipe (sign of the high word).
+__device__ __forceinline__ double clamp0(double x) { return (__double2hiint(x) < 0) ? 0.0 : x; }
+
 struct F64 {
     using R = double;
     struct C {
@@ -249,49 +252,49 @@ struct F64 {
         const double q02 = 1.0 - q00 - q01, q12 = 1.0 - q10 - q11;
         const double q20 = 1.0 - q00 - q10, q21 = 1.0 - q01 - q11;
         const double q22 = q00 + q01 + q10 + q11 - 1.0;
-        out[0] = q00; out[1] = q10; out[2] = fmax(q20, 0.0);
-        out[3] = q01; out[4] = q11; out[5] = fmax(q21, 0.0);
-        out[6] = fmax(q02, 0.0); out[7] = fmax(q12, 0.0); out[8] = fmax(q22, 0.0);
+        out[0] = q00; out[1] = q10; out[2] = clamp0(q20);
+        out[3] = q01; out[4] = q11; out[5] = clamp0(q21);
+        out[6] = clamp0(q02); out[7] = clamp0(q12); out[8] = clamp0(q22);
     }
     using Acc = double;
     static __device__ __forceinline__ double prob(C z) { return fma(z.re, z.re, z.im * z.im); }
     static __device__ __forceinline__ void complete_avg(double q00, double q01, double q10, double q11,
                                                         double out[9]) {
-        out[0] = q00; out[1] = q10; out[2] = fmax(1.0 - q00 - q10, 0.0);
-        out[3] = q01; out[4] = q11; out[5] = fmax(1.0 - q01 - q11, 0.0);
-        out[6] = fmax(1.0 - q00 - q01, 0.0); out[7] = fmax(1.0 - q10 - q11, 0.0);
-        out[8] = fmax(q00 + q01 + q10 + q11 - 1.0, 0.0);
+        out[0] = q00; out[1] = q10; out[2] = clamp0(1.0 - q00 - q10);
+        out[3] = q01; out[4] = q11; out[5] = clamp0(1.0 - q01 - q11);
+        out[6] = clamp0(1.0 - q00 - q01); out[7] = clamp0(1.0 - q10 - q11);
+        out[8] = clamp0(q00 + q01 + q10 + q11 - 1.0);
     }
 };
 
-// FP64 cos/sin of 2 pi u for |u| <= 1/2, from the 257-entry table tab[j + 128]
-// = (cos, sin)(2 pi j / 256): u = j / 256 + d with j = rint(256 u) (d exact,
-// |d| <= 1/512), x = 2 pi d, the Taylor series of sin x to x^7 and of
-// cos x - 1 to x^8 (truncation below 2e-23 for |x| <= pi/256), rotated onto
-// the table entry.  About 1 ulp; a third of the FP64 work of a general sincos.
-__device__ __forceinline__ void sincos_turns_f64(double u, const double2* __restrict__ tab, double& c,
+// FP64 cos/sin of 2 pi t for t in turns, |t| < 2^40.  j = round(256 t) comes
+// from adding 1.5 * 2^52 (the sum's low word is j mod 2^32), the remainder
+// d = t - j / 256 is exact (one FMA), and x = 2 pi d, |x| <= pi / 256, goes
+// through Taylor series of sin to x^5 and of cos - 1 to x^6 (truncation below
+// 1e-17) combined with entry (j + 128) mod 256 of the 257-entry table of
+// cos, sin of 2 pi (k - 128) / 256.  Sixteen FP64 instructions, the table
+// index on the integer pipe.
+__device__ __forceinline__ void sincos_turns_f64(double t, const double2* __restrict__ tab, double& c,
                                                  double& s) {
-    double j = rint(u * 256.0);
-    j = fmin(fmax(j, -128.0), 128.0);
-    const double d = fma(j, -0.00390625, u);
-    const double x = d * kTwoPi;
+    const double magic = 6755399441055744.0;  // 1.5 * 2^52
+    const double y = fma(t, 256.0, magic);
+    const int j = __double2loint(y);
+    const double jd = y - magic;
+    const double x = fma(jd, -0.00390625, t) * kTwoPi;
     const double x2 = x * x;
-    double p = fma(x2, -1.0 / 5040.0, 1.0 / 120.0);
-    p = fma(x2, p, -1.0 / 6.0);
+    const double p = fma(x2, 1.0 / 120.0, -1.0 / 6.0);
     const double sx = fma(x * x2, p, x);  // sin x
-    double q = fma(x2, 1.0 / 40320.0, -1.0 / 720.0);
-    q = fma(x2, q, 1.0 / 24.0);
+    double q = fma(x2, -1.0 / 720.0, 1.0 / 24.0);
     q = fma(x2, q, -0.5);
     const double cm1 = x2 * q;  // cos x - 1
-    const double2 e = tab[(int)j + 128];
-    c = e.x + fma(-e.y, sx, e.x * cm1);
-    s = e.y + fma(e.x, sx, e.y * cm1);
+    const double2 e = tab[(j + 128) & 255];
+    c = fma(-e.y, sx, fma(e.x, cm1, e.x));
+    s = fma(e.x, sx, fma(e.y, cm1, e.y));
 }
 
 // FP64 cos/sin of 2*pi*t, t = kappa * L turns.
 __device__ __forceinline__ void phase_f64(double kappa, double L, const double2* tab, double& c, double& s) {
-    const double t = kappa * L;
-    sincos_turns_f64(t - rint(t), tab, c, s);
+    sincos_turns_f64(kappa * L, tab, c, s);
 }
 
 }  // namespace cp3
