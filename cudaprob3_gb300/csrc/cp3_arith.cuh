@@ -267,20 +267,24 @@ struct F64 {
     }
 };
 
-// FP64 cos/sin of 2 pi t for t in turns, |t| < 2^40.  j = round(256 t) comes
-// from adding 1.5 * 2^52 (the sum's low word is j mod 2^32), the remainder
-// d = t - j / 256 is exact (one FMA), and x = 2 pi d, |x| <= pi / 256, goes
-// through Taylor series of sin to x^5 and of cos - 1 to x^6 (truncation below
-// 1e-17) combined with entry (j + 128) mod 256 of the 257-entry table of
-// cos, sin of 2 pi (k - 128) / 256.  Sixteen FP64 instructions, the table
-// index on the integer pipe.
-__device__ __forceinline__ void sincos_turns_f64(double t, const double2* __restrict__ tab, double& c,
-                                                 double& s) {
+// FP64 cos/sin of 2 pi t for t in turns, |t| < 2^40, in two steps.
+// reduce_turns_f64: j = round(256 t) from adding 1.5 * 2^52 (the sum's low
+// word is j mod 2^32) and the exact remainder d = t - j / 256 (one FMA),
+// |d| <= 1/512.  sincos_reduced_f64: x = 2 pi d, |x| <= pi / 256, through
+// Taylor series of sin to x^5 and of cos - 1 to x^6 (truncation below
+// 1e-17), rotated onto entry (j + 128) mod 256 of the 257-entry table of
+// cos, sin of 2 pi (k - 128) / 256.  Sixteen FP64 instructions in all, the
+// table index on the integer pipe.
+__device__ __forceinline__ void reduce_turns_f64(double t, int& j, double& d) {
     const double magic = 6755399441055744.0;  // 1.5 * 2^52
     const double y = fma(t, 256.0, magic);
-    const int j = __double2loint(y);
-    const double jd = y - magic;
-    const double x = fma(jd, -0.00390625, t) * kTwoPi;
+    j = __double2loint(y);
+    d = fma(y - magic, -0.00390625, t);
+}
+
+__device__ __forceinline__ void sincos_reduced_f64(int j, double d, const double2* __restrict__ tab, double& c,
+                                                   double& s) {
+    const double x = d * kTwoPi;
     const double x2 = x * x;
     const double p = fma(x2, 1.0 / 120.0, -1.0 / 6.0);
     const double sx = fma(x * x2, p, x);  // sin x
@@ -290,6 +294,14 @@ __device__ __forceinline__ void sincos_turns_f64(double t, const double2* __rest
     const double2 e = tab[(j + 128) & 255];
     c = fma(-e.y, sx, fma(e.x, cm1, e.x));
     s = fma(e.x, sx, fma(e.y, cm1, e.y));
+}
+
+__device__ __forceinline__ void sincos_turns_f64(double t, const double2* __restrict__ tab, double& c,
+                                                 double& s) {
+    int j;
+    double d;
+    reduce_turns_f64(t, j, d);
+    sincos_reduced_f64(j, d, tab, c, s);
 }
 
 // FP64 cos/sin of 2*pi*t, t = kappa * L turns.

@@ -179,20 +179,30 @@ struct F64Src {
         n1 = -s1;
         n2 = -s2;
     }
+    // Sum of phases in turns as (sum of the table indices j) / 256 + (sum of
+    // the exact remainders d): the integer part is exact, the remainders stay
+    // below 1/512 each.
     struct Turns {
-        double t = 0.0;  // reduced to [-1/2, 1/2]
+        unsigned j = 0;  // mod 2^32: only j mod 256 is read
+        double d = 0.0;
     };
     __device__ __forceinline__ void phase_acc(int l, double& c1, double& s1, double& n1, double& c2, double& s2,
                                               double& n2, Turns& acc) const {
-        phase(l, c1, s1, n1, c2, s2, n2);
         const double L = len[l];
         const double* k = tab + (l * kFp64Words + 9) * TE;
-        const double t1 = k[0] * L, t2 = k[TE] * L;
-        acc.t += (t1 - rint(t1)) + (t2 - rint(t2));
-        acc.t -= rint(acc.t);
+        int j1, j2;
+        double d1, d2;
+        reduce_turns_f64(k[0] * L, j1, d1);
+        reduce_turns_f64(k[TE] * L, j2, d2);
+        sincos_reduced_f64(j1, d1, ptab, c1, s1);
+        sincos_reduced_f64(j2, d2, ptab, c2, s2);
+        n1 = -s1;
+        n2 = -s2;
+        acc.j += (unsigned)j1 + (unsigned)j2;
+        acc.d += d1 + d2;
     }
     __device__ __forceinline__ void turns_phase(const Turns& acc, double& c, double& s) const {
-        sincos_turns_f64(acc.t, ptab, c, s);
+        sincos_turns_f64(fma((double)(int)(acc.j & 255u), 0.00390625, acc.d), ptab, c, s);
     }
 };
 
