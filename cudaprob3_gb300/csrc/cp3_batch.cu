@@ -9,11 +9,15 @@
 //
 // Device work:
 //   batch_prep_kernel       FP64 eigen data of every (set, energy, layer) and
-//                           segment lengths of every (set, cosine)
+//                           segment lengths of every (set, cosine, layer)
 //   batch_propagate_kernel  persistent: each block takes (set, energy tile,
 //                           cosine chunk) items from an atomic counter, largest
 //                           items first, and runs process_tile on them
-// The graph is: counter reset, prep, propagate.
+// The sets are split into up to 8 chunks of geometrically growing work; the
+// graph is a counter reset, then per chunk a prep launch on a low-priority
+// side stream and the chunk's persistent propagate launch on the
+// high-priority main stream, so that chunk k + 1's prep runs beside chunk k's
+// propagation.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -59,8 +63,10 @@ template <bool MIXED>
 __global__ void __launch_bounds__(256) batch_prep_kernel(BatchPrepArgs a) {
     extern __shared__ double s_v[];
     const int nl = a.nl;
-    if ((int)blockIdx.x < a.n_eblk) {
-        const int2 b = a.eblk[blockIdx.x];
+    // cosine blocks first: blocks dispatch in index order, and the short
+    // cosine blocks would otherwise trail the eigen-solves
+    if ((int)blockIdx.x >= a.n_cblk) {
+        const int2 b = a.eblk[blockIdx.x - a.n_cblk];
         const BatchGrid& gr = a.grids[b.x];
         const size_t word = MIXED ? 4 : 8;
         const GridTables g{(unsigned char*)a.tab + gr.tab_off * word, (unsigned char*)a.pe + gr.pe_off * word,
@@ -68,16 +74,31 @@ __global__ void __launch_bounds__(256) batch_prep_kernel(BatchPrepArgs a) {
         const int l = threadIdx.x, ey = threadIdx.y;
         const int e = b.y + ey;
         const bool live = (l < nl) && (e < gr.n_en_pad);
-        double* vme = s_v + ((size_t)ey * nl + (l < nl ? l : 0)) * 9;
-        if (live) {
-            const double E = a.energies[gr.en_off + (e < gr.n_en ? e : gr.n_en - 1)];
-            prep_energy_layer<MIXED>(gr.osc, E, a.rhoye[gr.rhoye_off + l], l, e, g, vme);
+        const int nt = nl * blockDim.y;
+        if (nt <= 32) {
+            // one warp: the next layer's eigenvectors come from the next lane,
+            // and the block needs no shared memory (so that it fits beside the
+            // persistent propagate blocks, which take nearly all of it)
+            double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, vn[9];
+            if (live) {
+                const double E = a.energies[gr.en_off + (e < gr.n_en ? e : gr.n_en - 1)];
+                prep_energy_layer<MIXED>(gr.osc, E, a.rhoye[gr.rhoye_off + l], l, e, g, v);
+            }
+            const unsigned mask = (nt == 32) ? 0xffffffffu : ((1u << nt) - 1u);
+#pragma unroll
+            for (int q = 0; q < 9; q++) vn[q] = __shfl_down_sync(mask, v[q], 1);
+            if (live) prep_overlap_v<MIXED>(l, e, g, v, vn);
+        } else {
+            double* vme = s_v + ((size_t)ey * nl + (l < nl ? l : 0)) * 9;
+            if (live) {
+                const double E = a.energies[gr.en_off + (e < gr.n_en ? e : gr.n_en - 1)];
+                prep_energy_layer<MIXED>(gr.osc, E, a.rhoye[gr.rhoye_off + l], l, e, g, vme);
+            }
+            __syncthreads();
+            if (live) prep_overlap<MIXED>(l, e, g, vme);
         }
-        __syncthreads();
-        if (live) prep_overlap<MIXED>(l, e, g, vme);
     } else {
-        const int bi = blockIdx.x - a.n_eblk;
-        const int2 b = a.cblk[bi];
+        const int2 b = a.cblk[blockIdx.x];
         const BatchGrid& gr = a.grids[b.x];
         // one thread per (cosine, layer): b.y is the block's first flat index
         const int f = b.y + threadIdx.y * blockDim.x + threadIdx.x;
@@ -193,7 +214,7 @@ static cudaError_t batch_prep_launch(bool mixed, const BatchPrepArgs& a, cudaStr
     const int blocks = a.n_eblk + a.n_cblk;
     if (blocks == 0) return cudaSuccess;
     dim3 block(a.nl, a.eb);
-    const size_t smem = (size_t)a.eb * a.nl * 9 * sizeof(double);
+    const size_t smem = (a.nl * a.eb <= 32) ? 0 : (size_t)a.eb * a.nl * 9 * sizeof(double);
     if (mixed)
         batch_prep_kernel<true><<<blocks, block, smem, s>>>(a);
     else
@@ -320,8 +341,7 @@ int build_layout(cp3_batch* b) {
     b->nl_pad = (b->nl + 1) / 2 * 2;
     const int W = b->mixed ? cp3::kMixedWords : cp3::kFp64Words;
     // one-warp prep blocks: they run beside the persistent propagate blocks,
-    // in the registers those leave free (3 x 256 threads x 80 registers of
-    // 65,536 leave room for one warp)
+    // in the registers and shared memory those leave free
     b->eb = std::max(1, 32 / b->nl);
     b->grids.assign(b->n_sets, cp3::BatchGrid{});
     b->eblk.clear();
@@ -348,6 +368,20 @@ int build_layout(cp3_batch* b) {
     std::vector<std::pair<double, int4>> work;
     double done = 0.0;
     int chunk = 0;
+    // chunk sizes grow geometrically (ratio 1.6): the first chunk's prep is
+    // the only one nothing hides, and every later chunk's prep, running in
+    // the room the previous chunk's persistent wave leaves, finishes within
+    // that chunk's propagation (measured: a prep co-running there proceeds
+    // at about twice the work rate of the propagation)
+    std::vector<double> bound(K, 1.0);
+    {
+        double sum = 0.0, w = 1.0;
+        for (int k = 0; k < K; k++, w *= 1.6) sum += w;
+        double acc = 0.0;
+        w = 1.0;
+        for (int k = 0; k < K; k++, w *= 1.6) bound[k] = (acc += w / sum);
+    }
+    auto boundary = [&](int k) { return bound[k]; };
     auto close_chunk = [&]() {
         std::stable_sort(work.begin(), work.end(),
                          [](const std::pair<double, int4>& x, const std::pair<double, int4>& y) { return x.first > y.first; });
@@ -384,7 +418,7 @@ int build_layout(cp3_batch* b) {
                 work.push_back({cost, make_int4(s, t, c0, ncl)});
             }
         done += set_cost[s];
-        if (chunk < K - 1 && done >= total_cost * (chunk + 1) / K) close_chunk();
+        if (chunk < K - 1 && done >= total_cost * boundary(chunk)) close_chunk();
     }
     close_chunk();
     b->n_chunks = chunk;
@@ -416,6 +450,10 @@ int build_layout(cp3_batch* b) {
     if (bps < 1) return bfail(CP3_ERR_LIMIT, "batch: launch shape does not fit on an SM");
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+    // one block per SM left free (when 5 or more fit) for the next chunk's
+    // prep blocks: the propagation alone measured the same at 5 or 6 blocks
+    // per SM, while going from 3 to 2 costs it 4 %
+    if (bps >= 5) bps--;
     b->blocks = std::max(1, sms * bps);  // per chunk: at most its item count
     b->layout_dirty = false;
     b->desc_dirty = true;
@@ -510,10 +548,16 @@ int capture(cp3_batch* b) {
     drop_graph(b);
     const int K = b->n_chunks;
     cudaStream_t cs = nullptr, side = nullptr;
-    std::vector<cudaEvent_t> evs(K + 1, nullptr);
-    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
-    if (!e) e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
-    for (int k = 0; k <= K && !e; k++) e = cudaEventCreateWithFlags(&evs[k], cudaEventDisableTiming);
+    std::vector<cudaEvent_t> evs(K + 2, nullptr);
+    // The propagate launches get the higher priority: the block scheduler then
+    // dispatches a chunk's persistent wave first and the next chunk's prep
+    // blocks (many small FP64 blocks) only into what the wave leaves free,
+    // instead of the prep flooding the SMs ahead of the propagation.
+    int lo_prio = 0, hi_prio = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
+    if (!e) e = cudaStreamCreateWithPriority(&cs, cudaStreamNonBlocking, hi_prio);
+    if (!e) e = cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, lo_prio);
+    for (int k = 0; k < K + 2 && !e; k++) e = cudaEventCreateWithFlags(&evs[k], cudaEventDisableTiming);
     auto cleanup = [&]() {
         for (cudaEvent_t ev : evs)
             if (ev) cudaEventDestroy(ev);
@@ -526,20 +570,25 @@ int capture(cp3_batch* b) {
     }
     e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     bool capturing = !e;
+    // Chunk k's propagation waits for its prep and for chunk k - 1's
+    // propagation (one stream): while it runs, chunk k + 1's prep fills the
+    // room its persistent wave leaves on every SM.  Letting chunk k + 1's
+    // propagation start early instead (a second stream) hands that room to
+    // propagate blocks and measured no faster.
     if (!e) e = cudaMemsetAsync(b->d_counter.p, 0, sizeof(int) * std::max(1, K), cs);
     if (!e) e = cudaEventRecord(evs[K], cs);  // fork
     if (!e) e = cudaStreamWaitEvent(side, evs[K], 0);
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
     for (int k = 0; k < K && !e; k++) {
         e = cp3::batch_prep_launch(b->mixed, prep_args(b, k), side);
         if (!e) e = cudaEventRecord(evs[k], side);
-        if (!e) e = cudaStreamWaitEvent(cs, evs[k], 0);  // joins the side stream at the last chunk
+        if (!e) e = cudaStreamWaitEvent(cs, evs[k], 0);
         const int n_items = b->chunk_items[k + 1] - b->chunk_items[k];
         if (!e && n_items > 0)
             e = cp3::batch_launch(b->mixed, b->te, prop_args(b, k), b->groups, b->smem, std::min(b->blocks, n_items),
                                   cs);
     }
+    if (!e) e = cudaEventRecord(evs[K + 1], side);  // join
+    if (!e) e = cudaStreamWaitEvent(cs, evs[K + 1], 0);
     cudaGraph_t g = nullptr;
     cudaError_t e2 = capturing ? cudaStreamEndCapture(cs, &g) : cudaSuccess;
     cleanup();
@@ -548,7 +597,7 @@ int capture(cp3_batch* b) {
         return bcuda(e ? e : e2, "graph capture");
     }
     b->graph = g;
-    if ((e = cudaGraphInstantiate(&b->exec, g, 0))) {
+    if ((e = cudaGraphInstantiate(&b->exec, g, cudaGraphInstantiateFlagUseNodePriority))) {
         drop_graph(b);
         return bcuda(e, "cudaGraphInstantiate");
     }

@@ -78,23 +78,32 @@ __device__ __forceinline__ void prep_energy_layer(const OscParams& osc, double E
     }
 }
 
-// Overlap pass of thread (l, e): T_l = V_{l+1}^T V_l from shared memory; the
-// innermost layer has no successor and keeps the identity.
+// Overlap pass of thread (l, e): T_l = V_{l+1}^T V_l from its own eigenvectors
+// v and the next layer's vn; the innermost layer has no successor and keeps
+// the identity.
 template <bool MIXED>
-__device__ __forceinline__ void prep_overlap(int l, int e, const GridTables& g, const double* vme) {
+__device__ __forceinline__ void prep_overlap_v(int l, int e, const GridTables& g, const double* v, const double* vn) {
     const int te = g.te, tile = e / te, lane = e % te;
     const int W = MIXED ? kMixedWords : kFp64Words;
     const size_t base = ((size_t)tile * g.nl + l) * W * te + lane;
-    const double* vn = vme + 9;
+#pragma unroll
     for (int i = 0; i < 3; i++)
+#pragma unroll
         for (int j = 0; j < 3; j++) {
-            const double tij = (l + 1 < g.nl) ? vn[i] * vme[j] + vn[3 + i] * vme[3 + j] + vn[6 + i] * vme[6 + j]
+            const double tij = (l + 1 < g.nl) ? vn[i] * v[j] + vn[3 + i] * v[3 + j] + vn[6 + i] * v[6 + j]
                                               : (i == j ? 1.0 : 0.0);
             if (MIXED)
                 ((int*)g.tab)[base + (size_t)(3 * i + j) * te] = q30_rn(tij);
             else
                 ((double*)g.tab)[base + (size_t)(3 * i + j) * te] = tij;
         }
+}
+
+// The same with the layers' eigenvectors in shared memory ([layer][9], the
+// next layer's right after this one's).
+template <bool MIXED>
+__device__ __forceinline__ void prep_overlap(int l, int e, const GridTables& g, const double* vme) {
+    prep_overlap_v<MIXED>(l, e, g, vme, vme + 9);
 }
 
 // Segment length of layer l of trajectory c (zero beyond M).  One thread per
