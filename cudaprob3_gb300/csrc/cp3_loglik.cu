@@ -80,6 +80,43 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
+// One halving step of a many-value warp sum: lanes with bit `off` clear keep
+// the first N/2 values and send the second half to their partner, the others
+// the reverse; each lane adds what it receives to what it keeps.
+template <int N, class T>
+__device__ __forceinline__ void warp_halve(T* v, int lane, int off) {
+    const bool hi = (lane & off) != 0;
+#pragma unroll
+    for (int i = 0; i < N / 2; i++) {
+        const T send = hi ? v[i] : v[i + N / 2];
+        const T keep = hi ? v[i + N / 2] : v[i];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+    }
+}
+
+// Sums of 16 values over the warp with 16 shuffles instead of 80 (recursive
+// halving): afterwards lanes 2q and 2q + 1 hold the total of value q in v[0].
+// A fixed order: deterministic.
+template <class T>
+__device__ __forceinline__ void warp_sum16(T (&v)[16], int lane) {
+    warp_halve<16>(v, lane, 16);
+    warp_halve<8>(v, lane, 8);
+    warp_halve<4>(v, lane, 4);
+    warp_halve<2>(v, lane, 2);
+    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+}
+
+// The same for 32 values (31 shuffles instead of 160): lane q holds the total
+// of value q in v[0].
+template <class T>
+__device__ __forceinline__ void warp_sum32(T (&v)[32], int lane) {
+    warp_halve<32>(v, lane, 16);
+    warp_halve<16>(v, lane, 8);
+    warp_halve<8>(v, lane, 4);
+    warp_halve<4>(v, lane, 2);
+    warp_halve<2>(v, lane, 1);
+}
+
 // e^{2 pi i t}, t = kappa * L turns; double: exact product and reduction;
 // float: double-float product, exact reduction, then FP32 sincospi.
 __device__ __forceinline__ Cx<double> phase_of(double kappa, double L) {
@@ -531,15 +568,16 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) ll_pair_kernel(LL
         // give zeros), in the kernel's precision: each term already carries
         // that precision's rounding, a 5-level tree adds at most 5 ulp of the
         // absolute sum
+        {
+            R v[16];
 #pragma unroll
-        for (int q = 0; q < 9; q++) {
-            const R v = warp_sum(tT[q]);
-            if (lane == 0) pl[(size_t)l * lstride + q] = v;
-        }
+            for (int q = 0; q < 9; q++) v[q] = tT[q];
+            v[9] = tk[0];
+            v[10] = tk[1];
 #pragma unroll
-        for (int k = 0; k < 2; k++) {
-            const R v = warp_sum(tk[k]);
-            if (lane == 0) pl[(size_t)l * lstride + 9 + k] = v;
+            for (int q = 11; q < 16; q++) v[q] = R(0);
+            warp_sum16(v, lane);
+            if ((lane & 1) == 0 && (lane >> 1) < kLLPerL) pl[(size_t)l * lstride + (lane >> 1)] = v[0];
         }
     }
     // layers above Mw are never crossed by this warp's cosines
@@ -548,21 +586,20 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) ll_pair_kernel(LL
             for (int q = 0; q < kLLPerL; q++) pl[(size_t)l * lstride + q] = R(0);
     // layer 0: T_0 and D_0
     {
+        R v[16];
 #pragma unroll
-        for (int q = 0; q < 9; q++) {
-            const R v = warp_sum(gT0[q / 3][q % 3]);
-            if (lane == 0) pl[q] = v;
-        }
+        for (int q = 0; q < 9; q++) v[q] = gT0[q / 3][q % 3];
 #pragma unroll
-        for (int k = 1; k < 3; k++) {
-            const R v = warp_sum(-twopi * src.L(0) * cjmul(gD0[k], D0[k]).im);
-            if (lane == 0) pl[9 + k - 1] = v;
-        }
+        for (int k = 1; k < 3; k++) v[9 + k - 1] = -twopi * src.L(0) * cjmul(gD0[k], D0[k]).im;
+#pragma unroll
+        for (int q = 11; q < 16; q++) v[q] = R(0);
+        warp_sum16(v, lane);
+        if ((lane & 1) == 0 && (lane >> 1) < kLLPerL) pl[lane >> 1] = v[0];
     }
     // per energy: Lambda', Gamma', LL
     R* pe = (R*)(std::is_same<R, float>::value ? (void*)a.part_e_f : (void*)a.part_e) +
             ((size_t)e * a.n_cchunk + cchunk) * kLLPerE;
-    R vals[kLLPerE - 1];
+    R vals[32];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         vals[k] = gLa[k];
@@ -572,13 +609,11 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) ll_pair_kernel(LL
         vals[12 + 2 * k] = gGb[k].re;
         vals[13 + 2 * k] = gGb[k].im;
     }
+    vals[kLLPerE - 1] = ll;
 #pragma unroll
-    for (int q = 0; q < kLLPerE - 1; q++) {
-        const R v = warp_sum(vals[q]);
-        if (lane == 0) pe[q] = v;
-    }
-    const R llw = warp_sum(ll);
-    if (lane == 0) pe[kLLPerE - 1] = llw;
+    for (int q = kLLPerE; q < 32; q++) vals[q] = R(0);
+    warp_sum32(vals, lane);
+    if (lane < kLLPerE) pe[lane] = vals[0];
 }
 
 // ---------------------------------------------------------- reduction ----
