@@ -152,10 +152,10 @@ CP3_HD double cubic_newton(double x, double a, double b, double g) {
     return x;
 }
 
-CP3_HD void eigvec_of(const double H[9], double m, double ma, double mb, double v[3]) {
-    // columns of N = (H - ma)(H - mb) are parallel to the eigenvector of m;
-    // take the one with the largest diagonal entry (H symmetric)
-    (void)m;
+// Column of N = (H - ma)(H - mb), which is parallel to the eigenvector of the
+// third eigenvalue: the column with the largest diagonal entry (H symmetric),
+// unnormalised.
+CP3_HD void projector_column(const double H[9], double ma, double mb, double c[3]) {
     const double a0 = H[0] - ma, a4 = H[4] - ma, a8 = H[8] - ma;
     const double b0 = H[0] - mb, b4 = H[4] - mb, b8 = H[8] - mb;
     const double n00 = a0 * b0 + H[1] * H[1] + H[2] * H[2];
@@ -167,19 +167,17 @@ CP3_HD void eigvec_of(const double H[9], double m, double ma, double mb, double 
     const double x0 = (p == 0) ? b0 : (p == 1) ? H[1] : H[2];
     const double x1 = (p == 1) ? b4 : (p == 0) ? H[1] : H[5];
     const double x2 = (p == 2) ? b8 : (p == 0) ? H[2] : H[5];
-    const double c0 = a0 * x0 + H[1] * x1 + H[2] * x2;
-    const double c1 = H[1] * x0 + a4 * x1 + H[5] * x2;
-    const double c2 = H[2] * x0 + H[5] * x1 + a8 * x2;
-    const double n2 = c0 * c0 + c1 * c1 + c2 * c2;
-    double inv = nonzero(n2) ? rsqrt_fp64(n2) : 0.0;
-    // deterministic sign: largest component positive
-    double big = c0;
-    if (abs_key(c1) > abs_key(big)) big = c1;
-    if (abs_key(c2) > abs_key(big)) big = c2;
-    if (sign_bit(big)) inv = -inv;
-    v[0] = c0 * inv;
-    v[1] = c1 * inv;
-    v[2] = c2 * inv;
+    c[0] = a0 * x0 + H[1] * x1 + H[2] * x2;
+    c[1] = H[1] * x0 + a4 * x1 + H[5] * x2;
+    c[2] = H[2] * x0 + H[5] * x1 + a8 * x2;
+}
+
+// Deterministic sign of an eigenvector: its largest component positive.
+CP3_HD bool negative_largest(const double c[3]) {
+    double big = c[0];
+    if (abs_key(c[1]) > abs_key(big)) big = c[1];
+    if (abs_key(c[2]) > abs_key(big)) big = c[2];
+    return sign_bit(big);
 }
 
 CP3_HD void layer_eigen(const OscParams& p, double E, double rhoye, double m[3], double V[9]) {
@@ -246,15 +244,27 @@ CP3_HD void layer_eigen(const OscParams& p, double E, double rhoye, double m[3],
     const bool cyc = ej >= ek;  // j = i+1, k = i+2 (cyclic) or j = i+2, k = i+1
     const int i = ri, j = cyc ? rj : rk;
     const double mje = cyc ? mj : mk, mke = cyc ? mk : mj;
+    // v_i normalised; v_j's column orthogonalised against v_i before its one
+    // normalisation (the sign of each from its column's largest component)
     double vi[3], vj[3], vk[3];
-    eigvec_of(H, mi, mje, mke, vi);
-    eigvec_of(H, mje, mke, mi, vj);
+    projector_column(H, mje, mke, vi);
+    projector_column(H, mke, mi, vj);
+    {
+        const double n2 = vi[0] * vi[0] + vi[1] * vi[1] + vi[2] * vi[2];
+        double inv = nonzero(n2) ? rsqrt_fp64(n2) : 0.0;
+        if (negative_largest(vi)) inv = -inv;
+        vi[0] *= inv;
+        vi[1] *= inv;
+        vi[2] *= inv;
+    }
+    const bool neg_j = negative_largest(vj);
     const double d = vj[0] * vi[0] + vj[1] * vi[1] + vj[2] * vi[2];
     vj[0] -= d * vi[0];
     vj[1] -= d * vi[1];
     vj[2] -= d * vi[2];
     const double nj2 = vj[0] * vj[0] + vj[1] * vj[1] + vj[2] * vj[2];
-    const double rj2 = nonzero(nj2) ? rsqrt_fp64(nj2) : 0.0;
+    double rj2 = nonzero(nj2) ? rsqrt_fp64(nj2) : 0.0;
+    if (neg_j) rj2 = -rj2;
     vj[0] *= rj2;
     vj[1] *= rj2;
     vj[2] *= rj2;
