@@ -1,0 +1,98 @@
+// Host build of the bit-level helpers and the eigen-solve of cp3_physics.cuh
+// (the same source the kernels use), checked against the conversions and
+// divisions they replace.  Prints "bad <count>" and exits non-zero on any
+// mismatch.
+#define CP3_HD inline
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <random>
+
+#include "cp3_physics.cuh"
+
+using namespace cp3;
+
+static long bad = 0;
+
+static void check_q30(double x) {
+    const long long want = std::llrint(x * 1073741824.0);  // round half to even
+    if (q30_rn(x) != (int)want && bad++ < 5) std::printf("q30_rn(%a) = %d, want %lld\n", x, q30_rn(x), want);
+}
+
+static void check_f32(double x) {
+    float want = (float)x;
+    if (std::fabs(x) < 1.1754943508222875e-38) want = std::copysign(0.0f, (float)x);  // flushed below FLT_MIN
+    const float got = f32_rn(x);
+    if (std::memcmp(&want, &got, 4) != 0 && bad++ < 5) std::printf("f32_rn(%a) = %a, want %a\n", x, (double)got, (double)want);
+    const float f = (float)x;
+    const double back = f64_of(f);
+    const double wantd = (std::fabs(f) < 1.17549435e-38f) ? std::copysign(0.0, (double)f) : (double)f;
+    if ((std::memcmp(&back, &wantd, 8) != 0) && bad++ < 5) std::printf("f64_of(%a) = %a\n", (double)f, back);
+}
+
+int main(int argc, char** argv) {
+    const long n = (argc > 1) ? std::atol(argv[1]) : 2000000;
+    std::mt19937_64 g(1);
+    std::uniform_real_distribution<double> u(-2.0, 2.0), cm(0.0, 1.3e9);
+    for (long i = 0; i < n; i++) {
+        const double x = u(g);
+        if (x > -2.0 && x < 2.0) check_q30(x);
+        check_f32(std::ldexp(x, (int)(g() % 80) - 40));
+        const double c = cm(g);
+        if (km_of_cm(c) != c / 1.0e5 && bad++ < 5) std::printf("km_of_cm(%a)\n", c);
+        const double a = std::ldexp(u(g), (int)(g() % 20) - 10), b = std::ldexp(u(g), (int)(g() % 20) - 10);
+        if (b != 0.0 && std::fabs(div_nr(a, b) - a / b) > 2.3e-16 * std::fabs(a / b) && bad++ < 5)
+            std::printf("div_nr(%a, %a)\n", a, b);
+        const double y = u(g), z = u(g);
+        if (less_than(y, z) != (y < z) && bad++ < 5) std::printf("less_than(%a, %a)\n", y, z);
+        if ((abs_key(y) >= abs_key(z)) != (std::fabs(y) >= std::fabs(z)) && bad++ < 5) std::printf("abs_key(%a)\n", y);
+    }
+    // ties of the Q1.30 rounding and halfway points between floats
+    for (long k = -3000; k < 3000; k++) {
+        check_q30((k + 0.5) / 1073741824.0);
+        check_q30(std::ldexp((double)k + 0.5, -40));
+        const double t = std::ldexp(1.0 + (2 * k + 1) * std::ldexp(1.0, -24), 3);
+        check_f32(t);
+        check_f32(-t);
+    }
+    const double edge[] = {0.0, -0.0, 1.0, -1.0, 1.9999999999, 1e-300, 1e-40, 3.4028235e38, 3.4028236e38, 1e39, -1e39};
+    for (double x : edge) {
+        if (std::fabs(x) < 2) check_q30(x);
+        check_f32(x);
+    }
+    if (!std::isnan(f32_rn(NAN)) || !std::isnan(f64_of(NAN))) bad++;
+    // eigen-solve: orthonormal, right-handed, eigen-pairs of 2E*H_r
+    OscParams o{};
+    fill_osc_params(o, 0.5837, 0.1496, 0.8587, 3.86, 7.42e-5, 2.51e-3, false);
+    for (int k = 0; k < 2000; k++) {
+        const double E = std::exp(std::log(0.1) + (std::log(1000.0) - std::log(0.1)) * (k % 200) / 199.0);
+        const double rhoye = (k / 200) * 1.4;
+        double m[3], V[9];
+        layer_eigen(o, E, rhoye, m, V);
+        const double fac = -(kGF * E * rhoye);
+        double H[9];
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++)
+                H[3 * i + j] = o.d1 * o.o[3 * i + 1] * o.o[3 * j + 1] + o.d2 * o.o[3 * i + 2] * o.o[3 * j + 2];
+        H[0] -= fac;
+        double worst = 0.0;
+        for (int c = 0; c < 3; c++) {
+            for (int i = 0; i < 3; i++) {
+                double hv = 0.0;
+                for (int j = 0; j < 3; j++) hv += H[3 * i + j] * V[3 * j + c];
+                worst = std::fmax(worst, std::fabs(hv - m[c] * V[3 * i + c]));
+            }
+            for (int d = 0; d < 3; d++) {
+                double dot = 0.0;
+                for (int i = 0; i < 3; i++) dot += V[3 * i + c] * V[3 * i + d];
+                worst = std::fmax(worst, std::fabs(dot - (c == d ? 1.0 : 0.0)) * 1e-2);
+            }
+        }
+        const double det = V[0] * (V[4] * V[8] - V[5] * V[7]) - V[1] * (V[3] * V[8] - V[5] * V[6]) +
+                           V[2] * (V[3] * V[7] - V[4] * V[6]);
+        if ((worst > 1e-15 || std::fabs(det - 1.0) > 1e-13) && bad++ < 5)
+            std::printf("layer_eigen E=%g rhoye=%g residual %g det %g\n", E, rhoye, worst, det);
+    }
+    std::printf("bad %ld\n", bad);
+    return bad != 0;
+}
