@@ -117,13 +117,12 @@ __device__ __forceinline__ void warp_sum32(T (&v)[32], int lane) {
     warp_halve<2>(v, lane, 1);
 }
 
-// e^{2 pi i t}, t = kappa * L turns; double: exact product and reduction;
-// float: double-float product, exact reduction, then FP32 sincospi.
-__device__ __forceinline__ Cx<double> phase_of(double kappa, double L) {
-    const double t = kappa * L;
-    const double r = t - rint(t);
-    double s, c;
-    sincospi(2.0 * r, &s, &c);
+// e^{2 pi i t}, t = kappa * L turns; double: the propagate kernels' FP64
+// phase (257-entry table, exact reduction, short Taylor series); float:
+// double-float product, exact reduction, then FP32 sincospi.
+__device__ __forceinline__ Cx<double> phase_of(double kappa, double L, const double2* __restrict__ tab) {
+    double c, s;
+    phase_f64(kappa, L, tab, c, s);
     return Cx<double>{c, s};
 }
 __device__ __forceinline__ Cx<float> phase_of(float2 kap, float2 L) {
@@ -177,6 +176,7 @@ struct LLArgs {
     float* tabf;     // tile-major [n_en_pad/32][nl][13][32]
     float* pef;      // [18][n_en_pad]
     float2* lenf;    // [n_cos][nl_pad], hi/lo
+    const double2* ptab;  // 257-entry FP64 phase table (cos, sin of 2 pi j / 256)
 };
 
 // ---------------------------------------------------------------- prep ----
@@ -261,11 +261,12 @@ template <>
 struct LLSrc<double> {
     LLTab tb;
     const double* len;  // this cosine's [nl_pad]
+    const double2* ptab;
     __device__ __forceinline__ LLSrc(const LLArgs& a, int e, int c)
-        : tb{a.tab, a.pe, e, a.nl, a.n_en_pad}, len(a.len + (size_t)c * a.nl_pad) {}
+        : tb{a.tab, a.pe, e, a.nl, a.n_en_pad}, len(a.len + (size_t)c * a.nl_pad), ptab(a.ptab) {}
     __device__ __forceinline__ double T(int l, int i, int j) const { return tb.T(l, i, j); }
     // e^{i psi_k} of layer l, k = 1, 2 (table words kappa_1, kappa_2)
-    __device__ __forceinline__ Cx<double> D(int l, int k) const { return phase_of(tb.kap(l, k - 1), len[l]); }
+    __device__ __forceinline__ Cx<double> D(int l, int k) const { return phase_of(tb.kap(l, k - 1), len[l], ptab); }
     __device__ __forceinline__ double L(int l) const { return len[l]; }
     __device__ __forceinline__ double pe(int w) const { return tb.pe_w(w); }
 };
@@ -946,6 +947,7 @@ struct cp3_loglik {
     double* d_eig = nullptr;
     float *d_tabf = nullptr, *d_pef = nullptr;
     float2* d_lenf = nullptr;
+    int4* d_ptab = nullptr;
     double* d_yel = nullptr;
     int *d_maxl = nullptr, *d_row = nullptr;
     cp3::OscParams* d_osc = nullptr;
@@ -968,7 +970,8 @@ void ll_free(cp3_loglik* L) {
     L->graph = nullptr;
     void* ptrs[] = {L->d_en, L->d_cos, L->d_radii, L->d_fe, L->d_fm, L->d_counts, L->d_tab, L->d_pe, L->d_len,
                     L->d_pl, L->d_pee, L->d_pg, L->d_yel, L->d_maxl, L->d_row, L->d_osc,
-                    L->d_eig, L->d_tabf, L->d_pef, L->d_lenf, L->d_plf, L->d_peef, L->d_fef, L->d_fmf, L->d_cntf};
+                    L->d_eig, L->d_tabf, L->d_pef, L->d_lenf, L->d_plf, L->d_peef, L->d_fef, L->d_fmf, L->d_cntf,
+                    L->d_ptab};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     L->d_en = L->d_cos = L->d_radii = L->d_fe = L->d_fm = L->d_counts = nullptr;
@@ -976,6 +979,7 @@ void ll_free(cp3_loglik* L) {
     L->d_eig = nullptr;
     L->d_tabf = L->d_pef = nullptr;
     L->d_lenf = nullptr;
+    L->d_ptab = nullptr;
     L->d_plf = L->d_peef = L->d_fef = L->d_fmf = L->d_cntf = nullptr;
     L->d_maxl = L->d_row = nullptr;
     L->d_osc = nullptr;
@@ -1026,6 +1030,7 @@ cp3::LLArgs ll_args(cp3_loglik* L, int type) {
     a.tabf = L->mixed ? L->d_tabf : nullptr;
     a.pef = L->mixed ? L->d_pef : nullptr;
     a.lenf = L->mixed ? L->d_lenf : nullptr;
+    a.ptab = (const double2*)L->d_ptab;
     a.part_l_f = L->mixed ? L->d_plf : nullptr;
     a.part_e_f = L->mixed ? L->d_peef : nullptr;
     a.flux_e_f = L->d_fef;
@@ -1072,6 +1077,11 @@ int ll_setup(cp3_loglik* L, int type) {
         (e = cudaMalloc((void**)&L->d_osc, kUpBytes)) ||
         (e = cudaMalloc(&L->d_eig, (size_t)L->n_en_pad * L->nl * cp3::kLLEigWords * 8)))
         return lcuda(e, "cudaMalloc(loglik)");
+    {
+        std::vector<int4> ptab(cp3::kPhaseTabN + 1);
+        cp3::fill_phase_table(false, ptab.data());
+        if ((e = dmalloc_copy(&L->d_ptab, ptab.data(), ptab.size()))) return lcuda(e, "loglik phase table");
+    }
     if (L->mixed) {
         std::vector<float> fe(L->flux_e.begin(), L->flux_e.end()), fm(L->flux_mu.begin(), L->flux_mu.end());
         std::vector<float> cnt(L->counts.begin(), L->counts.end());
