@@ -30,7 +30,8 @@ namespace cp3 {
 // Energy part: a block of (nl x eb) threads; thread (l, e) solves layer l at
 // energy e, the eigenvectors go through shared memory so that the same thread
 // can form the overlap T_l = V_{l+1}^T V_l.  Cosine part: one thread per
-// cosine, all segment lengths of that trajectory.
+// (cosine, layer) segment length, and the atmosphere segments of the
+// production heights spread over the cosine's layer threads.
 template <bool MIXED>
 __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a) {
     extern __shared__ double s_v[];  // [eb][nl][9]

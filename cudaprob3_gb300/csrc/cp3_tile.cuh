@@ -3,7 +3,8 @@
 //
 //   prep_energy_layer  FP64 eigen-solve of one (energy, layer) and the
 //                      mixed/FP64 table entries derived from it
-//   prep_cosine        segment lengths of one trajectory
+//   prep_overlap(_v)   T_l = V_{l+1}^T V_l of one (energy, layer)
+//   prep_cosine_layer  segment length of one (trajectory, layer)
 //   process_tile       one block's tile: TE energies x a chunk of cosines of
 //                      one grid -> 9 probability planes
 #pragma once
