@@ -93,6 +93,45 @@ int main(int argc, char** argv) {
         if ((worst > 1e-15 || std::fabs(det - 1.0) > 1e-13) && bad++ < 5)
             std::printf("layer_eigen E=%g rhoye=%g residual %g det %g\n", E, rhoye, worst, det);
     }
+    // random parameters, including exact degeneracies (dm21 = 0 or dm32 = 0:
+    // the 5e-9 eV^2 break), inverted ordering and vacuum layers
+    std::uniform_real_distribution<double> ang(0.0, 1.5707963), ph(0.0, 6.2831853), lg(0.0, 1.0);
+    double worst_res = 0.0, worst_orth = 0.0;
+    for (int k = 0; k < 200000; k++) {
+        const double dm21 = (k % 7 == 0) ? 0.0 : 7.4e-5 * (0.5 + lg(g));
+        const double dm32 = (k % 11 == 0) ? 0.0 : ((k & 1) ? -1.0 : 1.0) * 2.5e-3 * (0.5 + lg(g));
+        OscParams q{};
+        fill_osc_params(q, ang(g), ang(g), ang(g), ph(g), dm21, dm32, (k & 2) != 0);
+        const double E = std::exp(std::log(0.05) + lg(g) * (std::log(2000.0) - std::log(0.05)));
+        const double rhoye = (k % 5 == 0) ? 0.0 : 7.0 * lg(g);
+        double m[3], V[9];
+        layer_eigen(q, E, rhoye, m, V);
+        const double fac = q.anti ? kGF * E * rhoye : -(kGF * E * rhoye);
+        double H[9], hn = 0.0;
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                H[3 * i + j] = q.d1 * q.o[3 * i + 1] * q.o[3 * j + 1] + q.d2 * q.o[3 * i + 2] * q.o[3 * j + 2];
+                if (i == 0 && j == 0) H[0] -= fac;
+                hn = std::fmax(hn, std::fabs(H[3 * i + j]));
+            }
+        for (int c = 0; c < 3; c++) {
+            for (int i = 0; i < 3; i++) {
+                double hv = 0.0;
+                for (int j = 0; j < 3; j++) hv += H[3 * i + j] * V[3 * j + c];
+                worst_res = std::fmax(worst_res, std::fabs(hv - m[c] * V[3 * i + c]) / hn);
+            }
+            for (int d = 0; d < 3; d++) {
+                double dot = 0.0;
+                for (int i = 0; i < 3; i++) dot += V[3 * i + c] * V[3 * i + d];
+                worst_orth = std::fmax(worst_orth, std::fabs(dot - (c == d ? 1.0 : 0.0)));
+            }
+        }
+        const double det = V[0] * (V[4] * V[8] - V[5] * V[7]) - V[1] * (V[3] * V[8] - V[5] * V[6]) +
+                           V[2] * (V[3] * V[7] - V[4] * V[6]);
+        if (std::fabs(det - 1.0) > 1e-12 && bad++ < 5) std::printf("det %g at case %d\n", det, k);
+    }
+    std::printf("random cases: residual/|H| %.3g, |V^T V - I| %.3g\n", worst_res, worst_orth);
+    if (worst_res > 1e-11 || worst_orth > 1e-14) bad++;
     std::printf("bad %ld\n", bad);
     return bad != 0;
 }

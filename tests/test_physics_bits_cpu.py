@@ -4,7 +4,9 @@ conversions equal the hardware conversions they replace (Q1.30 rounding half
 to even, double to float and back, with the documented flush below FLT_MIN),
 the cm-to-km FMA correction equals the division, div_nr is within one ulp,
 the bit-pattern compares order like the FP64 compares, and the eigen-solve
-returns right-handed orthonormal eigen-pairs of 2E*H_r."""
+returns right-handed orthonormal eigen-pairs of 2E*H_r (200,000 random
+parameter sets with degeneracies, both orderings and vacuum layers:
+|HV - Vm| / |H| <= 1e-11, |V^T V - I| <= 1e-14, det V = 1)."""
 import os
 import shutil
 import subprocess
