@@ -131,11 +131,11 @@ def _probabilities(cos, en, body, params, rhos, device_id, height):
     return r[1], r[4]  # P(e -> mu), P(mu -> mu)
 
 
-def binned_problem(n_cos=400, n_en=200, device_id=0, seed=1, total=1.0e6):
+def binned_problem(n_cos=400, n_en=200, device_id=0, seed=1, total=1.0e6, body=None):
     cos = -1.0 + (np.arange(n_cos) + 0.5) / n_cos
     edges = np.exp(np.linspace(np.log(0.5), np.log(100.0), n_en + 1))
     en = np.sqrt(edges[:-1] * edges[1:])
-    body = G.PREM_12
+    body = G.PREM_12 if body is None else body
     flux_mu = en ** -2.7
     flux_e = 0.5 * flux_mu
     nominal = np.array(G.NOMINAL, dtype=np.float64)

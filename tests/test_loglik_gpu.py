@@ -58,6 +58,31 @@ def test_gradient_matches_finite_differences(problem, fd, precision, tol):
     assert g[6 + 0] == 0.0 and fd[6 + 0] == 0.0
 
 
+def _prem59():
+    import os
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "prem59.npz"))
+    return G.Body(d["radii"], d["rhos"], d["ye"])
+
+
+@pytest.mark.parametrize("body_name", ["prem4", "prem59"])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-4), ("mixed", 1e-3)])
+def test_gradient_other_bodies_ragged_grid(gpu, body_name, precision, tol):
+    """4 and 60 density rows (the layer kernel's packing: 6 energies per block
+    at 5 layers, one per block at 61), 50 x 30 bins (a partial cosine chunk
+    and a partial energy tile)."""
+    from cudaprob3_gb300.loglik import binned_problem
+    body = G.PREM_4 if body_name == "prem4" else _prem59()
+    prob = binned_problem(n_cos=50, n_en=30, body=body)
+    fd = fd_gradient(prob, prob.nominal, body.rhos)
+    with prob.make(precision=precision) as L:
+        ll, g = L.evaluate(prob.nominal, body.rhos)
+    want_ll = oracle_ll(prob, prob.nominal, body.rhos)
+    assert abs(ll - want_ll) <= (1e-9 if precision == "fp64" else 1e-6) * abs(want_ll) + 1e-6
+    assert g.shape == (6 + body.rhos.size,)
+    err = np.abs(g - fd) / np.linalg.norm(fd)
+    assert err.max() <= tol, "per-component error / |grad|: %s" % np.array2string(err, precision=2)
+
+
 def test_gradient_is_deterministic_and_moves_with_parameters(problem):
     with problem.make(precision="fp64") as L:
         a = L.evaluate(problem.nominal, problem.body.rhos)
