@@ -43,6 +43,40 @@ def test_batch_matches_oracle(gpu, precision, tol, anti):
         assert np.array_equal(b.results(), flat)
 
 
+def _prem59():
+    import os
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "prem59.npz"))
+    return G.Body(d["radii"], d["rhos"], d["ye"])
+
+
+@pytest.mark.parametrize("precision,tol", [("mixed", 1e-6), ("fp64", 1e-11)])
+@pytest.mark.parametrize("body_name", ["prem4", "prem59"])
+def test_batch_other_bodies(gpu, precision, tol, body_name):
+    """5 layers (prep blocks of one warp, neighbours by shuffles) and 61
+    layers (prep blocks of two warps, neighbours through shared memory)."""
+    from cudaprob3_gb300 import CP3Error
+    from cudaprob3_gb300.batch import BatchPropagator
+    nc, ne, params, scale, cos, en = make_sets(6, seed=11)
+    B = G.PREM_4 if body_name == "prem4" else _prem59()
+    with BatchPropagator(0, nc, ne, precision=precision) as b:
+        b.set_grids(cos, en)
+        b.set_parameters(params)
+        b.set_density(B.radii, B.rhos, B.ye, scale)
+        b.set_production_height(22.0)
+        if body_name == "prem59" and precision == "fp64":
+            # FP64 tables of 61 layers for a tile of 64 energies exceed shared
+            # memory: the handle says so, and a smaller tile fits
+            with pytest.raises(CP3Error, match="exceed shared memory"):
+                b.calculate(0)
+            b.set_launch_shape(32, 2, 16)
+        b.calculate(0)
+        flat = b.results()
+        for s in range(len(nc)):
+            got = b.set_result(flat, s).astype(np.float64)
+            want = oracle.calculate(cos[s], en[s], B.radii, B.rho_eff() * scale[s], tuple(params[s]), 22.0, False)
+            assert np.abs(got - want).max() <= tol, "set %d" % s
+
+
 def test_batch_autotune_and_shapes(gpu):
     from cudaprob3_gb300.batch import BatchPropagator
     nc, ne, params, scale, cos, en = make_sets(20, seed=7)
