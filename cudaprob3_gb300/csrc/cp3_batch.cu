@@ -340,6 +340,17 @@ int build_layout(cp3_batch* b) {
     b->nl = n + 1;
     b->nl_pad = (b->nl + 1) / 2 * 2;
     const int W = b->mixed ? cp3::kMixedWords : cp3::kFp64Words;
+    // the energy tile must leave room for the layer tables: halve the tile,
+    // then the cosine chunk, as the single-grid handle does
+    {
+        const size_t smem_max = (size_t)cp3::max_dynamic_smem();
+        auto need = [&]() { return cp3::tile_smem(b->mixed, b->te, b->nl, b->nl_pad, b->cchunk).total + 16; };
+        while (need() > smem_max && b->te > 32) {
+            b->te /= 2;
+            b->groups = std::min(b->groups * 2, cp3::propagate_max_threads(b->mixed) / b->te);
+        }
+        while (need() > smem_max && b->cchunk > 8) b->cchunk /= 2;
+    }
     // one-warp prep blocks: they run beside the persistent propagate blocks,
     // in the registers and shared memory those leave free
     b->eb = std::max(1, 32 / b->nl);
