@@ -483,8 +483,9 @@ def run_ours(args, world, rank, local):
                              "kernel_ms": fprop_ms, "work_per_launch": madw,
                              "achieved": madw / (fprop_ms * 1e-3) / 1e12, "peak": peak_dfma / 1e12,
                              "unit": "T DFMA/s", "frac": (madw / (fprop_ms * 1e-3)) / peak_dfma,
-                             "note": "chain multiply-adds only; the FP64 phases (sincospi) and the "
-                                     "completion come on top",
+                             "note": "chain multiply-adds only; the FP64 phases (257-entry table and "
+                                     "Taylor series, 16 FP64 instructions each) and the completion "
+                                     "come on top",
                              "peak_source": "measured live on this GPU (cp3_pipe_peak)"}}
         # precision of this step's mixed results against FP64 (every pair)
         for p, t in props:
