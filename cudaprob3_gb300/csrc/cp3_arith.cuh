@@ -149,32 +149,33 @@ struct Q30 {
 //      plus the cross terms;
 //   2. reduce: u = p - rint(p) (exact), j = rint(256 u), d = (u - j/256) + e,
 //      so t = integer + j/256 + d with |d| <= 1/512 (+ rounding);
-//   3. x = 2 pi d; sin x = x - x^3/6 and cos x - 1 = -x^2/2 + x^4/24 in FP32
-//      (truncation below 3e-12 for |x| <= pi/256);
+//   3. x = 2 pi d (2 pi as a float: 3.4e-10 rad at most); sin x = x - x^3/6
+//      and cos x - 1 = -x^2/2 + x^4/24 in FP32 (truncation below 3e-12 for
+//      |x| <= pi/256);
 //   4. rotate the table entry (C, S) = (cos, sin)(2 pi j/256) by x: the
 //      corrections C (cos x - 1) - S sin x and S (cos x - 1) + C sin x are
 //      below 0.013 in magnitude, so FP32 carries them to ~1e-9 absolute, and
 //      they are added to the exact Q1.30 table entry.
-// `tab` holds 257 entries (Q1.30 cos, Q1.30 sin, float cos, float sin) for
-// j = -128..128 at index j + 128.
+// `tab` holds 257 entries (Q1.30 cos, Q1.30 sin, float cos * 2^30, float
+// sin * 2^30: the corrections come out in Q1.30 units) for j = -128..128 at
+// index j + 128.  u lies in [-1/2, 1/2], so j = rint(256 u) is in range; a
+// NaN phase converts to j = 0.
 // Q1.30 cos/sin of 2 pi (p + e) for a phase given in turns as a double-float
 // pair (|e| small against 1): steps 2-4 above.
 __device__ __forceinline__ void turns_q30(float p, float e, const int4* __restrict__ tab, int& cq, int& sq) {
     const float u = p - rintf(p);
-    float j = rintf(u * 256.0f);
-    j = fminf(fmaxf(j, -128.0f), 128.0f);
+    const float j = rintf(u * 256.0f);
     const float d = fmaf(j, -0.00390625f, u) + e;
-    // 2*pi split as 6.28318548202514648 - 1.74845553e-7 (hi + lo = 2*pi to 2^-48)
-    const float x = fmaf(d, 6.28318548202514648f, d * -1.7484555314695172e-07f);
+    const float x = d * 6.28318548202514648f;
     const float x2 = x * x;
     const float sx = x * fmaf(x2, -0.16666666666666666f, 1.0f);
     const float cm = x2 * fmaf(x2, 0.041666666666666664f, -0.5f);
     const int4 t = tab[(int)j + 128];
     const float cf = __int_as_float(t.z), sf = __int_as_float(t.w);
-    const float dc = fmaf(cf, cm, -sf * sx);
+    const float dc = fmaf(cf, cm, -sf * sx);  // Q1.30 units
     const float ds = fmaf(sf, cm, cf * sx);
-    cq = t.x + __float2int_rn(dc * 1073741824.0f);
-    sq = t.y + __float2int_rn(ds * 1073741824.0f);
+    cq = t.x + __float2int_rn(dc);
+    sq = t.y + __float2int_rn(ds);
 }
 
 // t = (kh + kl) (Lh + Ll) turns as p + e: p = kh*Lh rounded, e its exact

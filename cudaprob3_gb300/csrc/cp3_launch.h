@@ -60,15 +60,15 @@ cudaError_t launch_propagate(bool mixed, const PropArgs& a, int te, int groups, 
                              cudaStream_t s, int mode = 0);
 
 // The 257-entry phase table of the propagate kernels, j = -128..128 at index
-// j + 128: mixed (Q1.30 cos, Q1.30 sin, float cos, float sin) of 2*pi*j/256;
-// FP64 (double cos, double sin) in the same 16 bytes.
+// j + 128: mixed (Q1.30 cos, Q1.30 sin, float cos * 2^30, float sin * 2^30)
+// of 2*pi*j/256; FP64 (double cos, double sin) in the same 16 bytes.
 inline void fill_phase_table(bool mixed, int4* tab) {
     for (int j = -kPhaseTabN / 2; j <= kPhaseTabN / 2; j++) {
         const double ang = kTwoPi * j / kPhaseTabN;
         const double c = std::cos(ang), s = std::sin(ang);
         int4& out = tab[j + kPhaseTabN / 2];
         if (mixed) {
-            const float cf = (float)c, sf = (float)s;
+            const float cf = (float)c * 1073741824.0f, sf = (float)s * 1073741824.0f;
             int ci, si;
             std::memcpy(&ci, &cf, 4);
             std::memcpy(&si, &sf, 4);

@@ -64,7 +64,8 @@ __global__ void noalloc_setup_kernel(NoAllocBody body, const double* cosines, in
         sincospi((double)(t - kPhaseTabN / 2) / (kPhaseTabN / 2), &s, &c);
         if (mixed)
             ptab[t] = make_int4((int)__double2ll_rn(c * 1073741824.0), (int)__double2ll_rn(s * 1073741824.0),
-                                __float_as_int(__double2float_rn(c)), __float_as_int(__double2float_rn(s)));
+                                __float_as_int(__double2float_rn(c) * 1073741824.0f),
+                                __float_as_int(__double2float_rn(s) * 1073741824.0f));
         else
             ((double2*)ptab)[t] = make_double2(c, s);
     }
