@@ -162,8 +162,7 @@ struct Q30 {
 // NaN phase converts to j = 0.
 // Q1.30 cos/sin of 2 pi (p + e) for a phase given in turns as a double-float
 // pair (|e| small against 1): steps 2-4 above.
-__device__ __forceinline__ void turns_q30(float p, float e, const int4* __restrict__ tab, int& cq, int& sq) {
-    const float u = p - rintf(p);
+__device__ __forceinline__ void turns_q30_u(float u, float e, const int4* __restrict__ tab, int& cq, int& sq) {
     const float j = rintf(u * 256.0f);
     const float d = fmaf(j, -0.00390625f, u) + e;
     const float x = d * 6.28318548202514648f;
@@ -176,6 +175,9 @@ __device__ __forceinline__ void turns_q30(float p, float e, const int4* __restri
     const float ds = fmaf(sf, cm, cf * sx);
     cq = t.x + __float2int_rn(dc);
     sq = t.y + __float2int_rn(ds);
+}
+__device__ __forceinline__ void turns_q30(float p, float e, const int4* __restrict__ tab, int& cq, int& sq) {
+    turns_q30_u(p - rintf(p), e, tab, cq, sq);
 }
 
 // t = (kh + kl) (Lh + Ll) turns as p + e: p = kh*Lh rounded, e its exact
@@ -194,17 +196,20 @@ __device__ __forceinline__ void phase_q30(float kh, float kl, float Lh, float Ll
     turns_q30(p, e, tab, cq, sq);
 }
 
-// Double-float running sum of phases in turns, kept reduced to [-1/2, 1/2]:
-// only e^{2 pi i sum} is needed, and the reduction keeps the pair exact.
+// Running sum of phases in turns as a Q0.32 fixed-point fraction: only
+// e^{2 pi i sum} is needed, so the sum is kept modulo one turn by the 32-bit
+// wrap-around.  Each phase adds its reduced part u (|u| <= 1/2) and its small
+// double-float remainder e, each rounded to 2^-32 turns.
 struct TurnSum {
-    float h = 0.0f, l = 0.0f;
-    __device__ __forceinline__ void add(float p, float e) {
-        p -= rintf(p);  // exact
-        const float s = h + p;
-        const float bp = s - h;
-        const float err = (h - (s - bp)) + (p - bp);  // two-sum
-        h = s - rintf(s);
-        l += err + e;
+    unsigned acc = 0u;
+    __device__ __forceinline__ void add(float u, float e) {
+        acc += (unsigned)__float2int_rn(u * 4294967296.0f) + (unsigned)__float2int_rn(e * 4294967296.0f);
+    }
+    // the sum as a reduced float u in [-1/2, 1/2) and its exact remainder e
+    __device__ __forceinline__ void split(float& u, float& e) const {
+        const int a = (int)acc;
+        u = (float)a * 2.3283064365386963e-10f;  // 2^-32
+        e = (float)(a - __float2int_rn(u * 4294967296.0f)) * 2.3283064365386963e-10f;
     }
 };
 

@@ -160,15 +160,18 @@ struct MixedSrc {
         float p1, e1, p2, e2;
         turns_product(__int_as_float(k[0]), __int_as_float(k[TE]), L.x, L.y, p1, e1);
         turns_product(__int_as_float(k[2 * TE]), __int_as_float(k[3 * TE]), L.x, L.y, p2, e2);
-        turns_q30(p1, e1, ptab, c1, s1);
-        turns_q30(p2, e2, ptab, c2, s2);
-        acc.add(p1, e1);
-        acc.add(p2, e2);
+        const float u1 = p1 - rintf(p1), u2 = p2 - rintf(p2);
+        turns_q30_u(u1, e1, ptab, c1, s1);
+        turns_q30_u(u2, e2, ptab, c2, s2);
+        acc.add(u1, e1);
+        acc.add(u2, e2);
         n1 = -s1;
         n2 = -s2;
     }
     __device__ __forceinline__ void turns_phase(const Turns& acc, int& c, int& s) const {
-        turns_q30(acc.h, acc.l, ptab, c, s);
+        float u, e;
+        acc.split(u, e);
+        turns_q30_u(u, e, ptab, c, s);
     }
 };
 
