@@ -372,7 +372,7 @@ def run_ours(args, world, rank, local):
     # DRAM bytes (read + write) of one propagate_kernel<mixed> launch at
     # 4096 x 4096 from an ncu capture of that launch (dram__bytes_read.sum +
     # dram__bytes_write.sum; summary in profiles/propagate_mixed_4096x4096_ncu.md)
-    traffic = 547_718_400 if (NC, NE) == (4096, 4096) else None
+    traffic = 548_889_600 if (NC, NE) == (4096, 4096) else None
     roofline = {
         "bound": "fma-pipe (mad.wide.s32 integer MAC on the FMA-heavy pipe)",
         "achieved": madw / (prop_ms * 1e-3) / 1e12, "peak": peak_madw / 1e12, "unit": "Tops/s",
