@@ -269,9 +269,13 @@ def test_configs1_scale_mixed_vs_fp64(gpu):
         t = gpu.Antineutrino if anti else gpu.Neutrino
         pf.calculateProbabilities(t)
         pm.calculateProbabilities(t)
-        d = (bm.double() - bf).abs()
+        ds = bm.double() - bf
+        d = ds.abs()
         assert float(d.max()) <= 1e-6
         assert float(d.mean()) <= 1e-7
+        # no systematic drift per channel from the chain's floor rounding
+        # (measured <= 5.5e-9; the float32 output rounding alone averages 6e-9)
+        assert float(ds.view(9, -1).mean(1).abs().max()) <= 2e-8
         want = oracle.calculate(c[idx], e[idx], B.radii, B.rho_eff(), G.NOMINAL, 22.0, anti)
         gf = bf.cpu().numpy()[:, idx][:, :, idx]
         assert np.abs(gf - want).max() <= 1e-11
