@@ -86,6 +86,18 @@ def test_ragged_sizes(gpu, precision, nc, ne):
     assert np.abs(got - want).max() <= TOL[precision]
 
 
+@pytest.mark.parametrize("precision,anti", [("fp64", False), ("mixed", False), ("mixed", True)])
+def test_low_energies(gpu, precision, anti):
+    """0.1 MeV - 0.1 GeV: phases of up to 1e5 turns across the Earth, where the
+    double-float remainder of the mixed kernel's phase product reaches the
+    table step (its Taylor correction still holds down to 0.1 MeV)."""
+    c = G.linspace(-1, 0, 64)
+    e = G.logspace(1e-4, 0.1, 40)
+    got = run(gpu, precision, c, e, G.PREM_12.radii, G.PREM_12.rhos, G.PREM_12.ye, G.NOMINAL, anti=anti)
+    want = oracle.calculate(c, e, G.PREM_12.radii, G.PREM_12.rho_eff(), G.NOMINAL, 22.0, anti)
+    assert np.abs(got - want).max() <= (1e-9 if precision == "fp64" else TOL[precision])
+
+
 def test_empty_grid(gpu):
     with gpu.CudaPropagatorSingle(0, 0, 16) as p:
         p.setEnergyList(G.logspace(1, 10, 16))
