@@ -165,10 +165,10 @@ struct Q30 {
 __device__ __forceinline__ void turns_q30_u(float u, float e, const int4* __restrict__ tab, int& cq, int& sq) {
     const float j = rintf(u * 256.0f);
     const float d = fmaf(j, -0.00390625f, u) + e;
-    const float x = d * 6.28318548202514648f;
-    const float x2 = x * x;
-    const float sx = x * fmaf(x2, -0.16666666666666666f, 1.0f);
-    const float cm = x2 * fmaf(x2, 0.041666666666666664f, -0.5f);
+    // sin(2 pi d) and cos(2 pi d) - 1 with 2 pi folded into the coefficients
+    const float d2 = d * d;
+    const float sx = d * fmaf(d2, -4.134170224e+01f, 6.283185307e+00f);
+    const float cm = d2 * fmaf(d2, 6.493939402e+01f, -1.973920880e+01f);
     const int4 t = tab[(int)j + 128];
     const float cf = __int_as_float(t.z), sf = __int_as_float(t.w);
     const float dc = fmaf(cf, cm, -sf * sx);  // Q1.30 units
@@ -281,11 +281,12 @@ struct F64 {
 // FP64 cos/sin of 2 pi t for t in turns, |t| < 2^40, in two steps.
 // reduce_turns_f64: j = round(256 t) from adding 1.5 * 2^52 (the sum's low
 // word is j mod 2^32) and the exact remainder d = t - j / 256 (one FMA),
-// |d| <= 1/512.  sincos_reduced_f64: x = 2 pi d, |x| <= pi / 256, through
+// |d| <= 1/512.  sincos_reduced_f64: with x = 2 pi d, |x| <= pi / 256, the
 // Taylor series of sin to x^5 and of cos - 1 to x^6 (truncation below
-// 1e-17), rotated onto entry (j + 128) mod 256 of the 257-entry table of
-// cos, sin of 2 pi (k - 128) / 256.  Sixteen FP64 instructions in all, the
-// table index on the integer pipe.
+// 1e-17), written in d with 2 pi folded into the coefficients, rotated onto
+// entry (j + 128) mod 256 of the 257-entry table of cos, sin of
+// 2 pi (k - 128) / 256.  Fifteen FP64 instructions in all, the table index on
+// the integer pipe.
 __device__ __forceinline__ void reduce_turns_f64(double t, int& j, double& d) {
     const double magic = 6755399441055744.0;  // 1.5 * 2^52
     const double y = fma(t, 256.0, magic);
@@ -295,13 +296,14 @@ __device__ __forceinline__ void reduce_turns_f64(double t, int& j, double& d) {
 
 __device__ __forceinline__ void sincos_reduced_f64(int j, double d, const double2* __restrict__ tab, double& c,
                                                    double& s) {
-    const double x = d * kTwoPi;
-    const double x2 = x * x;
-    const double p = fma(x2, 1.0 / 120.0, -1.0 / 6.0);
-    const double sx = fma(x * x2, p, x);  // sin x
-    double q = fma(x2, -1.0 / 720.0, 1.0 / 24.0);
-    q = fma(x2, q, -0.5);
-    const double cm1 = x2 * q;  // cos x - 1
+    // sin(2 pi d) and cos(2 pi d) - 1 with 2 pi folded into the coefficients
+    const double d2 = d * d;
+    double p = fma(d2, 81.60524927607506, -41.34170224039976);
+    p = fma(d2, p, 6.283185307179586);
+    const double sx = d * p;
+    double q = fma(d2, -85.45681720669373, 64.9393940226683);
+    q = fma(d2, q, -19.739208802178716);
+    const double cm1 = d2 * q;
     const double2 e = tab[(j + 128) & 255];
     c = fma(-e.y, sx, fma(e.x, cm1, e.x));
     s = fma(e.x, sx, fma(e.y, cm1, e.y));
