@@ -372,7 +372,7 @@ def run_ours(args, world, rank, local):
     # DRAM bytes (read + write) of one propagate_kernel<mixed> launch at
     # 4096 x 4096 from an ncu capture of that launch (dram__bytes_read.sum +
     # dram__bytes_write.sum; summary in profiles/propagate_mixed_4096x4096_ncu.md)
-    traffic = 548_889_600 if (NC, NE) == (4096, 4096) else None
+    traffic = 549_239_552 if (NC, NE) == (4096, 4096) else None
     roofline = {
         "bound": "fma-pipe (mad.wide.s32 integer MAC on the FMA-heavy pipe)",
         "achieved": madw / (prop_ms * 1e-3) / 1e12, "peak": peak_madw / 1e12, "unit": "Tops/s",
@@ -484,7 +484,7 @@ def run_ours(args, world, rank, local):
                              "achieved": madw / (fprop_ms * 1e-3) / 1e12, "peak": peak_dfma / 1e12,
                              "unit": "T DFMA/s", "frac": (madw / (fprop_ms * 1e-3)) / peak_dfma,
                              "note": "chain multiply-adds only; the FP64 phases (257-entry table and "
-                                     "Taylor series, 16 FP64 instructions each) and the completion "
+                                     "Taylor series, 15 FP64 instructions each) and the completion "
                                      "come on top",
                              "peak_source": "measured live on this GPU (cp3_pipe_peak)"}}
         # precision of this step's mixed results against FP64 (every pair)
