@@ -60,13 +60,13 @@ struct BatchPrepArgs {
 };
 
 template <bool MIXED>
-__global__ void __launch_bounds__(256) batch_prep_kernel(BatchPrepArgs a) {
+__device__ __forceinline__ void batch_prep_item(const BatchPrepArgs& a, int bid) {
     extern __shared__ double s_v[];
     const int nl = a.nl;
     // cosine blocks first: blocks dispatch in index order, and the short
     // cosine blocks would otherwise trail the eigen-solves
-    if ((int)blockIdx.x >= a.n_cblk) {
-        const int2 b = a.eblk[blockIdx.x - a.n_cblk];
+    if ((int)bid >= a.n_cblk) {
+        const int2 b = a.eblk[bid - a.n_cblk];
         const BatchGrid& gr = a.grids[b.x];
         const size_t word = MIXED ? 4 : 8;
         const GridTables g{(unsigned char*)a.tab + gr.tab_off * word, (unsigned char*)a.pe + gr.pe_off * word,
@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(256) batch_prep_kernel(BatchPrepArgs a) {
             if (live) prep_overlap<MIXED>(l, e, g, vme);
         }
     } else {
-        const int2 b = a.cblk[blockIdx.x];
+        const int2 b = a.cblk[bid];
         const BatchGrid& gr = a.grids[b.x];
         // one thread per (cosine, layer): b.y is the block's first flat index
         const int f = b.y + threadIdx.y * blockDim.x + threadIdx.x;
@@ -109,6 +109,15 @@ __global__ void __launch_bounds__(256) batch_prep_kernel(BatchPrepArgs a) {
                            (unsigned char*)a.len + gr.len_off * 8, gr.n_en_pad, a.te, nl, a.nl_pad};
         prep_cosine_layer<MIXED>(a.cosines[gr.cos_off + c], a.maxl[gr.cos_off + c], a.radii, a.height_cm, c, l, g);
     }
+}
+
+// A grid of at most a few blocks per SM loops over the prep items: the items
+// run beside the persistent propagate wave of the previous chunk, and fewer,
+// longer-lived blocks keep the block scheduler out of its way.
+template <bool MIXED>
+__global__ void __launch_bounds__(256) batch_prep_kernel(BatchPrepArgs a) {
+    const int n = a.n_eblk + a.n_cblk;
+    for (int bid = blockIdx.x; bid < n; bid += gridDim.x) batch_prep_item<MIXED>(a, bid);
 }
 
 struct BatchPropArgs {
@@ -210,9 +219,9 @@ static cudaError_t batch_occupancy(bool mixed, int te, int groups, size_t smem, 
     return cudaErrorInvalidValue;
 }
 
-static cudaError_t batch_prep_launch(bool mixed, const BatchPrepArgs& a, cudaStream_t s) {
-    const int blocks = a.n_eblk + a.n_cblk;
-    if (blocks == 0) return cudaSuccess;
+static cudaError_t batch_prep_launch(bool mixed, const BatchPrepArgs& a, cudaStream_t s, int max_blocks) {
+    const int blocks = std::min(a.n_eblk + a.n_cblk, std::max(1, max_blocks));
+    if (a.n_eblk + a.n_cblk == 0) return cudaSuccess;
     dim3 block(a.nl, a.eb);
     const size_t smem = (a.nl * a.eb <= 32) ? 0 : (size_t)a.eb * a.nl * 9 * sizeof(double);
     if (mixed)
@@ -555,6 +564,11 @@ cp3::BatchPropArgs prop_args(cp3_batch* b, int k) {
 // Capture: counter reset, then per chunk k a prep launch on a side stream and
 // the persistent propagate of chunk k on the main stream after it, so that
 // chunk k + 1's FP64 prep overlaps chunk k's propagation.
+// Blocks per SM of the looping prep launches (measured on the 1024-set batch:
+// 2 leave the prep exposed, 55.0 ms per step; 4 51.6 ms; 8 51.9 ms; one block
+// per item, about 100,000 per chunk, 52.0 ms).
+constexpr int kPrepBlocksPerSM = 4;
+
 int capture(cp3_batch* b) {
     drop_graph(b);
     const int K = b->n_chunks;
@@ -586,11 +600,14 @@ int capture(cp3_batch* b) {
     // room its persistent wave leaves on every SM.  Letting chunk k + 1's
     // propagation start early instead (a second stream) hands that room to
     // propagate blocks and measured no faster.
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+    const int prep_grid = std::max(1, sms) * kPrepBlocksPerSM;
     if (!e) e = cudaMemsetAsync(b->d_counter.p, 0, sizeof(int) * std::max(1, K), cs);
     if (!e) e = cudaEventRecord(evs[K], cs);  // fork
     if (!e) e = cudaStreamWaitEvent(side, evs[K], 0);
     for (int k = 0; k < K && !e; k++) {
-        e = cp3::batch_prep_launch(b->mixed, prep_args(b, k), side);
+        e = cp3::batch_prep_launch(b->mixed, prep_args(b, k), side, prep_grid);
         if (!e) e = cudaEventRecord(evs[k], side);
         if (!e) e = cudaStreamWaitEvent(cs, evs[k], 0);
         const int n_items = b->chunk_items[k + 1] - b->chunk_items[k];
