@@ -22,8 +22,8 @@
 //                     over energies: sums the warps' partials and
 //                     back-propagates through the layer's FP64
 //                     eigen-decomposition to the parameters
-//   ll_sum_kernel     one block per output: sums the per-energy rows (fixed
-//                     order: deterministic)
+// The per-energy rows land in mapped host memory; the host sums them over the
+// energies in a fixed order (deterministic) after the graph completes.
 // Precision: FP64 does every step in double; MIXED runs ll_pair_kernel in
 // FP32 (phases in double-float) with the FP64 tables, sums its float partials
 // over the cosine chunks by compensated FP32 sums and does the eigen
@@ -71,13 +71,6 @@ __device__ __forceinline__ Cx<T> cj(Cx<T> a) { return Cx<T>{a.re, -a.im}; }
 template <class T>
 __device__ __forceinline__ Cx<T> cjmul(Cx<T> a, Cx<T> b) {
     return Cx<T>{a.re * b.re + a.im * b.im, a.re * b.im - a.im * b.re};
-}
-
-template <class T>
-__device__ __forceinline__ T warp_sum(T v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
 }
 
 // One halving step of a many-value warp sum: lanes with bit `off` clear keep
@@ -165,8 +158,7 @@ struct LLArgs {
     const float* flux_mu_f;
     const float* counts_f;
     float norm_f;
-    double* part_g;  // [n_en][7 + n_rows]: per-energy LL and gradient
-    double* out;     // [1 + 6 + nrows]: LL, gradient
+    double* part_g;  // [n_en][7 + n_rows]: per-energy LL and gradient (mapped host memory)
     const int* layer_row;  // [nl]: caller's row of layer l (l >= 1), -1 for layer 0
     int n_rows;
     const double* ye_layer;  // [nl]
@@ -884,21 +876,6 @@ __global__ void __launch_bounds__(288) ll_layer_kernel(LLArgs a, int epb) {
             a.part_g[(size_t)e * (7 + a.n_rows) + t] = (sRow[t] + sRow[kLLOscOut + t]) + sRow[2 * kLLOscOut + t];
 }
 
-// Block q sums output slot q over the energies: threads stride the energies,
-// then warp butterflies and the warps in order; the order is fixed, the sum
-// deterministic.  One slot per block spreads the FP64 adds over the SMs.
-__global__ void __launch_bounds__(128) ll_sum_kernel(LLArgs a) {
-    __shared__ double s_w[4];
-    const int np1 = 7 + a.n_rows, q = blockIdx.x;
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double v = 0.0;
-    for (int e = threadIdx.x; e < a.n_en; e += 128) v += a.part_g[(size_t)e * np1 + q];
-    v = warp_sum(v);
-    if (lane == 0) s_w[w] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) a.out[q] = ((s_w[0] + s_w[1]) + s_w[2]) + s_w[3];
-}
-
 }  // namespace cp3
 
 // ======================================================================= host
@@ -942,7 +919,6 @@ struct cp3_loglik {
     // device
     double *d_en = nullptr, *d_cos = nullptr, *d_radii = nullptr, *d_fe = nullptr, *d_fm = nullptr, *d_counts = nullptr;
     double *d_tab = nullptr, *d_pe = nullptr, *d_len = nullptr, *d_pl = nullptr, *d_pee = nullptr;
-    double* d_pg = nullptr;
     float *d_plf = nullptr, *d_peef = nullptr, *d_fef = nullptr, *d_fmf = nullptr, *d_cntf = nullptr;
     double* d_eig = nullptr;
     float *d_tabf = nullptr, *d_pef = nullptr;
@@ -952,10 +928,11 @@ struct cp3_loglik {
     int *d_maxl = nullptr, *d_row = nullptr;
     cp3::OscParams* d_osc = nullptr;
     // pinned staging [OscParams, cmat][rhoye], uploaded by one copy into d_osc;
-    // h_out is mapped: ll_sum_kernel writes the results there directly
+    // h_rows is mapped [n_en][7 + n_rows]: ll_layer_kernel writes each
+    // energy's log-likelihood and gradient terms there directly
     unsigned char* h_up = nullptr;
-    double* h_out = nullptr;
-    double* dh_out = nullptr;
+    double* h_rows = nullptr;
+    double* dh_rows = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int graph_type = -1;
@@ -969,13 +946,13 @@ void ll_free(cp3_loglik* L) {
     L->exec = nullptr;
     L->graph = nullptr;
     void* ptrs[] = {L->d_en, L->d_cos, L->d_radii, L->d_fe, L->d_fm, L->d_counts, L->d_tab, L->d_pe, L->d_len,
-                    L->d_pl, L->d_pee, L->d_pg, L->d_yel, L->d_maxl, L->d_row, L->d_osc,
+                    L->d_pl, L->d_pee, L->d_yel, L->d_maxl, L->d_row, L->d_osc,
                     L->d_eig, L->d_tabf, L->d_pef, L->d_lenf, L->d_plf, L->d_peef, L->d_fef, L->d_fmf, L->d_cntf,
                     L->d_ptab};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     L->d_en = L->d_cos = L->d_radii = L->d_fe = L->d_fm = L->d_counts = nullptr;
-    L->d_tab = L->d_pe = L->d_len = L->d_pl = L->d_pee = L->d_pg = L->d_yel = nullptr;
+    L->d_tab = L->d_pe = L->d_len = L->d_pl = L->d_pee = L->d_yel = nullptr;
     L->d_eig = nullptr;
     L->d_tabf = L->d_pef = nullptr;
     L->d_lenf = nullptr;
@@ -1025,7 +1002,7 @@ cp3::LLArgs ll_args(cp3_loglik* L, int type) {
     a.len = L->d_len;
     a.part_l = L->d_pl;
     a.part_e = L->d_pee;
-    a.part_g = L->d_pg;
+    a.part_g = L->dh_rows;
     a.eig = L->d_eig;
     a.tabf = L->mixed ? L->d_tabf : nullptr;
     a.pef = L->mixed ? L->d_pef : nullptr;
@@ -1037,7 +1014,6 @@ cp3::LLArgs ll_args(cp3_loglik* L, int type) {
     a.flux_mu_f = L->d_fmf;
     a.counts_f = L->d_cntf;
     a.norm_f = (float)L->norm;
-    a.out = L->dh_out;
     a.layer_row = L->d_row;
     a.n_rows = L->n_rows;
     a.ye_layer = L->d_yel;
@@ -1073,7 +1049,6 @@ int ll_setup(cp3_loglik* L, int type) {
     const size_t pee = (size_t)L->n_cchunk * L->n_en * cp3::kLLPerE;
     if ((e = cudaMalloc(&L->d_tab, tab * 8)) || (e = cudaMalloc(&L->d_pe, pe * 8)) || (e = cudaMalloc(&L->d_len, len * 8)) ||
         (e = cudaMalloc(&L->d_pl, pl * 8)) || (e = cudaMalloc(&L->d_pee, pee * 8)) ||
-        (e = cudaMalloc(&L->d_pg, (size_t)L->n_en * (cp3::kLLMaxParams + 1) * 8)) ||
         (e = cudaMalloc((void**)&L->d_osc, kUpBytes)) ||
         (e = cudaMalloc(&L->d_eig, (size_t)L->n_en_pad * L->nl * cp3::kLLEigWords * 8)))
         return lcuda(e, "cudaMalloc(loglik)");
@@ -1137,10 +1112,6 @@ int ll_setup(cp3_loglik* L, int type) {
         cp3::ll_layer_kernel<<<(L->n_en + epb - 1) / epb, threads, smem, cs>>>(a, epb);
         e = cudaGetLastError();
     }
-    if (!e) {
-        cp3::ll_sum_kernel<<<7 + L->n_rows, 128, 0, cs>>>(a);
-        e = cudaGetLastError();
-    }
     cudaGraph_t g = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(cs, &g);
     cudaStreamDestroy(cs);
@@ -1177,8 +1148,9 @@ int cp3_loglik_create(cp3_loglik** out, int device_id, int precision, int n_cos,
     cudaError_t e;
     if ((e = cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking)) ||
         (e = cudaMallocHost((void**)&L->h_up, kUpBytes)) ||
-        (e = cudaHostAlloc((void**)&L->h_out, sizeof(double) * (cp3::kLLMaxParams + 1), cudaHostAllocMapped)) ||
-        (e = cudaHostGetDevicePointer((void**)&L->dh_out, L->h_out, 0))) {
+        (e = cudaHostAlloc((void**)&L->h_rows, sizeof(double) * (size_t)n_en * (cp3::kLLMaxParams + 1),
+                           cudaHostAllocMapped)) ||
+        (e = cudaHostGetDevicePointer((void**)&L->dh_rows, L->h_rows, 0))) {
         int rc = lcuda(e, "loglik create");
         cp3_loglik_destroy(L);
         return rc;
@@ -1193,7 +1165,7 @@ int cp3_loglik_destroy(cp3_loglik* L) {
     if (L->stream) cudaStreamSynchronize(L->stream);
     ll_free(L);
     if (L->h_up) cudaFreeHost(L->h_up);
-    if (L->h_out) cudaFreeHost(L->h_out);
+    if (L->h_rows) cudaFreeHost(L->h_rows);
     if (L->stream) cudaStreamDestroy(L->stream);
     delete L;
     return CP3_OK;
@@ -1320,9 +1292,17 @@ int cp3_loglik_evaluate(cp3_loglik* L, int type, const double* params, const dou
     cudaError_t e = cudaGraphLaunch(L->exec, L->stream);
     if (!e) e = cudaStreamSynchronize(L->stream);
     if (e) return lcuda(e, "loglik evaluation");
-    if (loglik) *loglik = L->h_out[0];
+    // fixed-order sums of the energies' rows (slot 0 the log-likelihood, then
+    // the 6 oscillation parameters and the density rows)
+    const int np1 = 7 + L->n_rows;
+    double s[cp3::kLLMaxParams + 1] = {};
+    for (int en = 0; en < L->n_en; en++) {
+        const double* row = L->h_rows + (size_t)en * np1;
+        for (int q = 0; q < np1; q++) s[q] += row[q];
+    }
+    if (loglik) *loglik = s[0];
     if (grad)
-        for (int q = 0; q < 6 + L->n_rows; q++) grad[q] = L->h_out[1 + q];
+        for (int q = 0; q < 6 + L->n_rows; q++) grad[q] = s[1 + q];
     return CP3_OK;
 }
 
