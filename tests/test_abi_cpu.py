@@ -56,3 +56,27 @@ def test_create_without_device():
 def test_bad_precision_rejected():
     with pytest.raises(ValueError):
         cp.CudaPropagatorSingle(0, 8, 8, precision="half")
+
+
+def product_files():
+    """Every source file of the shipped product: package, kernels, headers."""
+    for top in ("cudaprob3_gb300", "include"):
+        for d, _, files in os.walk(os.path.join(ROOT, top)):
+            if "__pycache__" in d:
+                continue
+            for f in files:
+                if f.endswith((".py", ".cu", ".cuh", ".h", ".hpp", ".cpp")):
+                    yield os.path.join(d, f)
+
+
+def test_product_never_touches_the_oracle():
+    # the oracle is the checker of tests and the CPU legs of bench.py only
+    hits = [p for p in product_files() if re.search(r"\boracle\b", open(p).read())]
+    assert not hits, hits
+
+
+def test_missing_library_fails_loudly(monkeypatch):
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib, "LIB_PATH", os.path.join(ROOT, "no_such_dir", "libcudaprob3_gb300.so"))
+    with pytest.raises(ImportError, match="not built"):
+        _lib.load()
