@@ -66,9 +66,14 @@ struct Q30 {
     // Two's-complement sums are exact in any order, so the results are
     // bit-identical to the chained form.
 
-    // z * e where e = (c, s); ns = -s is not needed in this form
+    // z * e where e = (c, s), by Gauss's three products: k1 = c (re + im),
+    // re = k1 - im (c + s), im = k1 + re (s - c); c + s and s - c are shared
+    // by every rotation with the same phase.  All operands stay below 2 in
+    // magnitude (|z|, |e| <= 1), and the integer sums are exact, so the result
+    // equals the four-product form bit for bit.
     __device__ __forceinline__ C mulPhase(C z, int c, int s, int /*ns*/) const {
-        return C{rnd(mulb(z.re, c) - mul(z.im, s)), rnd(mulb(z.im, c) + mul(z.re, s))};
+        const long long k1 = mulb(c, z.re + z.im);
+        return C{rnd(k1 - mul(z.im, c + s)), rnd(k1 + mul(z.re, s - c))};
     }
     // t0 z0 + t1 z1 + t2 z2
     __device__ __forceinline__ C dotRC(R t0, R t1, R t2, C z0, C z1, C z2) const {

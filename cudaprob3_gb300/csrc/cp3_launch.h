@@ -83,7 +83,7 @@ inline void fill_phase_table(bool mixed, int4* tab) {
 // Message returned by cp3_last_error() on this thread.
 void set_last_error(const std::string& msg);
 
-// Throughput of one pipe on the current device (0 mad.wide.s32, 1 FFMA, 2 DFMA).
+// Throughput of one pipe on the current device (0 mul.wide.s32, 1 FFMA, 2 DFMA).
 cudaError_t measure_pipe(int pipe, double* ops_per_second);
 
 }  // namespace cp3

@@ -221,7 +221,8 @@ int cp3_last_kernel_ms(cp3_propagator* p, float* prep_ms, float* propagate_ms);
 
 /* Measured throughput of one GPU pipe on `device`, in operations per second
  * (no reference counterpart; it gives the roofline denominators):
- *   CP3_PIPE_IMAD_WIDE  mad.wide.s32 (32x32+64 -> 64), the Q1.30 chain's MAC
+ *   CP3_PIPE_IMAD_WIDE  32x32 -> 64 integer products (mul.wide.s32), the
+ *                       Q1.30 chain's multiply
  *   CP3_PIPE_FFMA       FP32 fused multiply-add
  *   CP3_PIPE_DFMA       FP64 fused multiply-add                                */
 #define CP3_PIPE_IMAD_WIDE 0
