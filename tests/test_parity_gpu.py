@@ -295,3 +295,17 @@ def test_configs1_scale_mixed_vs_fp64(gpu):
         assert float((s.sum(0) - 1).abs().max()) <= 1e-6
     pf.close()
     pm.close()
+
+
+def test_pipe_peaks_are_plausible(gpu):
+    """The roofline denominators: each probe returns a rate between a tenth of
+    and twice the nominal GB300 figure at 2.07 GHz on 152 SMs (32 integer
+    products, 128 FP32 FMAs, ~1.7 FP64 FMAs per clock per SM)."""
+    from cudaprob3_gb300 import _lib
+    from cudaprob3_gb300.propagator import pipe_peak
+
+    nominal = {_lib.PIPE_IMAD_WIDE: 32, _lib.PIPE_FFMA: 128, _lib.PIPE_DFMA: 1.7}
+    for pipe, per_clk in nominal.items():
+        rate = pipe_peak(pipe, 0)
+        ref = per_clk * 152 * 2.07e9
+        assert 0.1 * ref < rate < 2.0 * ref, (pipe, rate, ref)
