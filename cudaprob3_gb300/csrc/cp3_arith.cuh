@@ -81,19 +81,26 @@ struct Q30 {
         const long long i = (mulb(t0, z0.im) + mul(t1, z1.im)) + mul(t2, z2.im);
         return C{rnd(r), rnd(i)};
     }
+    // a b as (k1 - k3) + i (k1 + k2), Gauss's three products (exact)
+    static __device__ __forceinline__ void gauss(C a, C b, long long& re, long long& im) {
+        const long long k1 = mul(b.re, a.re + a.im);
+        re = k1 - mul(a.im, b.re + b.im);
+        im = k1 + mul(a.re, b.im - b.re);
+    }
     // a0 b0 + a1 b1 + a2 b2 (complex)
     __device__ __forceinline__ C dotCC(C a0, C a1, C a2, C b0, C b1, C b2) const {
-        const long long r = ((mulb(a0.re, b0.re) - mul(a0.im, b0.im)) + (mul(a1.re, b1.re) - mul(a1.im, b1.im))) +
-                            (mul(a2.re, b2.re) - mul(a2.im, b2.im));
-        const long long i = ((mulb(a0.re, b0.im) + mul(a0.im, b0.re)) + (mul(a1.re, b1.im) + mul(a1.im, b1.re))) +
-                            (mul(a2.re, b2.im) + mul(a2.im, b2.re));
-        return C{rnd(r), rnd(i)};
+        long long r0, i0, r1, i1, r2, i2;
+        gauss(a0, b0, r0, i0);
+        gauss(a1, b1, r1, i1);
+        gauss(a2, b2, r2, i2);
+        return C{rnd((r0 + r1) + r2), rnd((i0 + i1) + i2)};
     }
     // conj(a0 b1 - a1 b0): one component of conj(u x v)
     __device__ __forceinline__ C crossConj(C a0, C a1, C b0, C b1) const {
-        const long long r = (mulb(a0.re, b1.re) - mul(a0.im, b1.im)) - (mul(a1.re, b0.re) - mul(a1.im, b0.im));
-        const long long i = (mul(a1.re, b0.im) + mul(a1.im, b0.re)) - (mulb(a0.re, b1.im) + mul(a0.im, b1.re));
-        return C{rnd(r), rnd(i)};
+        long long r0, i0, r1, i1;
+        gauss(a0, b1, r0, i0);
+        gauss(a1, b0, r1, i1);
+        return C{rnd(r0 - r1), rnd(i1 - i0)};
     }
     // |z|^2 exactly, as Q2.60 in 64 bits
     static __device__ __forceinline__ long long norm2(C z) { return mul(z.re, z.re) + mul(z.im, z.im); }
