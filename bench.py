@@ -372,7 +372,7 @@ def run_ours(args, world, rank, local):
     # DRAM bytes (read + write) of one propagate_kernel<mixed> launch at
     # 4096 x 4096 from an ncu capture of that launch (dram__bytes_read.sum +
     # dram__bytes_write.sum; summary in profiles/propagate_mixed_4096x4096_ncu.md)
-    traffic = 545_915_648 if (NC, NE) == (4096, 4096) else None
+    traffic = 547_799_552 if (NC, NE) == (4096, 4096) else None
     roofline = {
         "bound": "fma-pipe (mul.wide.s32 integer products on the FMA-heavy pipe)",
         "achieved": prods / (prop_ms * 1e-3) / 1e12, "peak": peak_prod / 1e12, "unit": "Tops/s",
