@@ -3,7 +3,8 @@
 //   Q30  : mixed path.  Amplitudes, eigen-bases and overlaps are Q1.30 fixed
 //          point (int32, value = x / 2^30, |x| < 2); each 3-term complex dot
 //          product is summed exactly in 64 bits from mul.wide.s32 products
-//          (32x32 -> 64 on the FMA-heavy pipe) and is rounded once, down
+//          (32x32 -> 64 on the FMA-heavy pipe; complex products by Gauss's
+//          three multiplications) and is rounded once, down
 //          (floor, one funnel shift; the overlap tables alternate in sign from
 //          layer to layer so that these one-sided errors do not add up along
 //          the chain).  Phases are
@@ -81,7 +82,11 @@ struct Q30 {
         const long long i = (mulb(t0, z0.im) + mul(t1, z1.im)) + mul(t2, z2.im);
         return C{rnd(r), rnd(i)};
     }
-    // a b as (k1 - k3) + i (k1 + k2), Gauss's three products (exact)
+    // a b by Gauss's three products: k1 = b.re (a.re + a.im),
+    // k2 = a.re (b.im - b.re), k3 = a.im (b.re + b.im); a b = (k1 - k3) +
+    // i (k1 + k2), exactly.  Every operand of the chain's complex products is
+    // an entry of a unitary matrix or of a unit vector (|a|, |b| <= 1), so the
+    // pre-adds stay below 2 and fit Q1.30.
     static __device__ __forceinline__ void gauss(C a, C b, long long& re, long long& im) {
         const long long k1 = mul(b.re, a.re + a.im);
         re = k1 - mul(a.im, b.re + b.im);
