@@ -80,3 +80,17 @@ def test_missing_library_fails_loudly(monkeypatch):
     monkeypatch.setattr(_lib, "LIB_PATH", os.path.join(ROOT, "no_such_dir", "libcudaprob3_gb300.so"))
     with pytest.raises(ImportError, match="not built"):
         _lib.load()
+
+
+def test_binding_arity_matches_header():
+    """Every ctypes signature has as many arguments as the C declaration."""
+    text = "".join(open(h).read() for h in HEADERS)
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    decls = re.findall(r"(?:int|const char\s*\*)\s+(cp3_\w+)\s*\(([^)]*)\)\s*;", text, re.S)
+    assert decls
+    arity = {n: len(args) for n, _, args in _lib.SIGNATURES}
+    for name, params in decls:
+        p = params.strip()
+        n = 0 if p in ("", "void") else p.count(",") + 1
+        assert arity[name] == n, (name, n, arity[name])
