@@ -95,11 +95,14 @@ def grid():
 
 # ------------------------------------------------------------- work units --
 def products_per_pair(M):
-    """32x32 -> 64 integer products (mul.wide.s32) one pair executes in the mixed kernel
-    (flavour_block in cp3_chain.cuh): 52 per inner chain step T_l D_l on two
-    columns, 36 to rebuild the third column, and the fixed cost of D_0 Gamma',
-    T_0 (.), G = Y^T D_M Y, G X', Lambda' X and the four exact |S|^2 of the
-    2x2 flavour block."""
+    """32x32 -> 64 integer products (mul.wide.s32) of one pair in the mixed
+    kernel's algorithm (flavour_block in cp3_chain.cuh), every complex product
+    counted as four real ones: 52 per inner chain step T_l D_l on two columns,
+    36 to rebuild the third column, and the fixed cost of D_0 Gamma', T_0 (.),
+    G = Y^T D_M Y, G X', Lambda' X and the four exact |S|^2 of the 2x2 flavour
+    block.  The kernel forms complex products with Gauss's three products, so
+    it executes fewer (48 per inner step); the roofline counts this fixed
+    algorithmic work."""
     M = np.asarray(M, dtype=np.int64)
     return np.where(M >= 2, 52 * M + 198, np.where(M == 1, 260, 68))
 
