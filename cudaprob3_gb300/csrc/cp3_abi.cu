@@ -345,6 +345,8 @@ int cp3_set_cosine_list(cp3_propagator* p, const double* list, int n) {
         if (!(list[i] >= -1.0 && list[i] <= 1.0))
             return fail(CP3_ERR_ARGUMENT, "setCosineList: cosines must lie in [-1, 1]");
     p->cosines.assign(list, list + n);
+    // propagator.hpp:266-268 re-sets the height through km, a round trip that
+    // can move it by one ulp; kept so that path lengths match bit for bit
     if (p->is_set_height) p->height_cm = (p->height_cm / 100000.0) * 100000.0;
     set_maxlayers(p);
     p->is_set_cosine = true;
