@@ -235,9 +235,11 @@ int cp3_pipe_peak(int device, int pipe, double* ops_per_second);
  * has its own oscillation parameters, density scale and grid of
  * n_cosines[s] x n_energies[s] pairs, and its results are the reference's
  * [9][n_cosines[s]][n_energies[s]] planes at element offset offsets[s].  One
- * calculation is one CUDA-graph launch: a counter reset, one FP64 precompute
- * kernel over all sets and one persistent kernel that takes (set, energy
- * tile, cosine chunk) work items, largest first.  No reference counterpart
+ * calculation is one CUDA-graph launch: a counter reset, then the sets in up
+ * to 8 chunks of growing work, each an FP64 precompute kernel on a
+ * low-priority branch and a persistent kernel on the high-priority one that
+ * takes (set, energy tile, cosine chunk) work items, largest first; the
+ * precompute of chunk k + 1 runs beside the propagation of chunk k.  No reference counterpart
  * (the reference evaluates one parameter point per calculateProbabilities).
  * Errors are reported through cp3_last_error() like the single-grid ABI. */
 typedef struct cp3_batch cp3_batch;
