@@ -382,35 +382,18 @@ int cp3_set_density(cp3_propagator* p, const double* radii, const double* rhos, 
     if (!radii || !rhos) return fail(CP3_ERR_ARGUMENT, "setDensity : null array");
     if (n > CP3_MAX_ROWS)
         return fail(CP3_ERR_LIMIT, "setDensity : more than " + std::to_string(CP3_MAX_ROWS) + " rows");
-    for (int i = 0; i < n; i++) {
-        if (!std::isfinite(radii[i]) || !std::isfinite(rhos[i]) || radii[i] < 0.0 || rhos[i] < 0.0)
-            return fail(CP3_ERR_ARGUMENT, "setDensity : radii and densities must be finite and >= 0");
-        if (ye && !(ye[i] >= 0.0 && ye[i] <= 1.0))
-            return fail(CP3_ERR_ARGUMENT, "setDensity : electron fractions must lie in [0, 1]");
-    }
-    // propagator.hpp:127-147: one monotone order, flipped to outside-in
-    bool flip = false;
-    if (n >= 2) {
-        const int sign = (radii[1] - radii[0] > 0 ? 1 : -1);
-        for (int i = 1; i < n; i++)
-            if ((radii[i] - radii[i - 1]) * sign < 0) return fail(CP3_ERR_ARGUMENT, "radii order messed up");
-        flip = (sign == 1);
-    }
+    // propagator.hpp:127-158: one monotone order, flipped to outside-in; cosine limits
+    cp3::BodyRow rows[CP3_MAX_ROWS];
+    if (const char* msg = cp3::order_body(radii, rhos, ye, n, rows)) return fail(CP3_ERR_ARGUMENT, msg);
     p->radii.resize(n);
     p->rhos.resize(n);
     p->ye.resize(n);
-    for (int i = 0; i < n; i++) {
-        const int s = flip ? n - 1 - i : i;
-        p->radii[i] = radii[s];
-        p->rhos[i] = rhos[s];
-        p->ye[i] = ye ? ye[s] : 0.5;
-    }
-    // propagator.hpp:149-158
     p->coslimit.resize(n);
     for (int i = 0; i < n; i++) {
-        double x = -1 * std::sqrt(1 - (p->radii[i] * p->radii[i] / (cp3::kREarth * cp3::kREarth)));
-        if (i == 0) x = 0;
-        p->coslimit[i] = x;
+        p->radii[i] = rows[i].radius;
+        p->rhos[i] = rows[i].rho;
+        p->ye[i] = rows[i].ye;
+        p->coslimit[i] = rows[i].coslimit;
     }
     set_maxlayers(p);
     p->has_density = true;
@@ -942,17 +925,6 @@ int cp3_last_kernel_ms(cp3_propagator* p, float* prep_ms, float* prop_ms) {
     if (e != cudaSuccess) return cuda_fail(e, "cudaEventElapsedTime");
     if (prep_ms) *prep_ms = a;
     if (prop_ms) *prop_ms = b;
-    return CP3_OK;
-}
-
-int cp3_pipe_peak(int device, int pipe, double* ops) {
-    if (!ops) return fail(CP3_ERR_ARGUMENT, "null output pointer");
-    if (pipe < 0 || pipe > 2) return fail(CP3_ERR_ARGUMENT, "unknown pipe");
-    if (device < 0 || device >= cp3_device_count()) return fail(CP3_ERR_NO_DEVICE, "No GPU found");
-    DeviceGuard g(device);
-    if (g.err != cudaSuccess) return cuda_fail(g.err, "cudaSetDevice");
-    cudaError_t e = cp3::measure_pipe(pipe, ops);
-    if (e != cudaSuccess) return cuda_fail(e, "pipe probe");
     return CP3_OK;
 }
 

@@ -168,12 +168,7 @@ __global__ void __launch_bounds__(MIXED ? 256 : 128, MIXED ? 4 : 3) batch_propag
 
 template <bool MIXED, int TE>
 static cudaError_t batch_attr() {
-    static bool done = false;
-    if (done) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(batch_propagate_kernel<MIXED, TE>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem());
-    if (e == cudaSuccess) done = true;
-    return e;
+    return opt_in_max_smem((const void*)batch_propagate_kernel<MIXED, TE>);
 }
 
 template <bool MIXED, int TE>

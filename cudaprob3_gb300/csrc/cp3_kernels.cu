@@ -19,7 +19,10 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
+#include <set>
 #include <type_traits>
+#include <utility>
 
 #include "cp3_launch.h"
 #include "cp3_tile.cuh"
@@ -140,15 +143,23 @@ cudaError_t launch_prep(bool mixed, PrepArgs a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+cudaError_t opt_in_max_smem(const void* func) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    static std::mutex mu;
+    static std::set<std::pair<const void*, int>> done;  // (kernel, device) pairs already opted in
+    std::lock_guard<std::mutex> lock(mu);
+    if (done.count({func, dev})) return cudaSuccess;
+    e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem());
+    if (e == cudaSuccess) done.insert({func, dev});
+    return e;
+}
+
 template <bool MIXED, int TE, int MODE>
 static cudaError_t launch_prop_t(const PropArgs& a, int groups, size_t smem, cudaStream_t s) {
-    static bool configured = false;  // one attribute call per instantiation (per process)
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(propagate_kernel<MIXED, TE, MODE>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic_smem());
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+    cudaError_t e = opt_in_max_smem((const void*)propagate_kernel<MIXED, TE, MODE>);
+    if (e != cudaSuccess) return e;
     dim3 grid(a.n_en_pad / TE, (a.n_cos + a.cchunk - 1) / a.cchunk);
     dim3 block(TE, groups);
     propagate_kernel<MIXED, TE, MODE><<<grid, block, smem, s>>>(a);

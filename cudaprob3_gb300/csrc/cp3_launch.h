@@ -51,6 +51,13 @@ size_t propagate_smem_bytes(bool mixed, int te, int nl, int nl_pad, int cchunk);
 // Largest dynamic shared memory a block of the current device may opt in to.
 int max_dynamic_smem();
 
+// Opts kernel `func` in to max_dynamic_smem() bytes of dynamic shared memory
+// on the current device.  A function attribute belongs to one device's
+// context, so the opt-in is made once per (kernel, device) -- not once per
+// process -- under a lock, so that handles on several devices and several
+// host threads may launch the same kernel.
+cudaError_t opt_in_max_smem(const void* func);
+
 // Largest block (threads) the propagate kernel of a precision accepts.
 inline int propagate_max_threads(bool mixed) { return mixed ? 256 : 128; }
 cudaError_t launch_prep(bool mixed, PrepArgs a, cudaStream_t s);
@@ -80,10 +87,44 @@ inline void fill_phase_table(bool mixed, int4* tab) {
     }
 }
 
+// One density row after Propagator::setDensity's reordering: outermost first.
+struct BodyRow {
+    double radius, rho, ye;
+    double coslimit;  // cosine below which a trajectory enters this shell
+};
+
+// Propagator::setDensity (propagator.hpp:117-161) for n >= 1 rows given in
+// either monotone order: checks the values (finite, >= 0, ye in [0, 1]; ye
+// may be null for 0.5 everywhere), flips an ascending list to outside-in, and
+// forms coslimit[i] = -sqrt(1 - r_i^2 / R^2) with coslimit[0] = 0.  Writes n
+// rows into `out` and returns nullptr, or returns the error message (the
+// reference's text where it has one) and leaves `out` undefined.
+inline const char* order_body(const double* radii, const double* rhos, const double* ye, int n, BodyRow* out) {
+    for (int i = 0; i < n; i++) {
+        if (!std::isfinite(radii[i]) || !std::isfinite(rhos[i]) || radii[i] < 0.0 || rhos[i] < 0.0)
+            return "setDensity : radii and densities must be finite and >= 0";
+        if (ye && !(ye[i] >= 0.0 && ye[i] <= 1.0)) return "setDensity : electron fractions must lie in [0, 1]";
+    }
+    bool flip = false;
+    if (n >= 2) {
+        const int sign = (radii[1] - radii[0] > 0 ? 1 : -1);
+        for (int i = 1; i < n; i++)
+            if ((radii[i] - radii[i - 1]) * sign < 0) return "radii order messed up";
+        flip = (sign == 1);
+    }
+    for (int i = 0; i < n; i++) {
+        const int s = flip ? n - 1 - i : i;
+        out[i].radius = radii[s];
+        out[i].rho = rhos[s];
+        out[i].ye = ye ? ye[s] : 0.5;
+        double x = -1 * std::sqrt(1 - (out[i].radius * out[i].radius / (kREarth * kREarth)));
+        if (i == 0) x = 0;
+        out[i].coslimit = x;
+    }
+    return nullptr;
+}
+
 // Message returned by cp3_last_error() on this thread.
 void set_last_error(const std::string& msg);
-
-// Throughput of one pipe on the current device (0 mul.wide.s32, 1 FFMA, 2 DFMA).
-cudaError_t measure_pipe(int pipe, double* ops_per_second);
 
 }  // namespace cp3

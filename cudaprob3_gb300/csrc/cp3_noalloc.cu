@@ -1,22 +1,28 @@
 // One calculation that allocates nothing: cp3_propagate_noalloc.
 //
-// Some callers cannot call cudaMalloc: code that runs while a stream is being
-// captured into a CUDA graph (allocation is not a capturable operation),
-// callers inside a framework whose caching allocator must own every device
-// byte, and latency-bound or real-time loops that may not take the implicit
-// device synchronisation of cudaMalloc/cudaFree.  For them this entry point
-// runs the single-grid calculation (precompute, then propagation) on the
-// caller's device pointers and stream, with its scratch tables in a
-// file-scope __device__ array instead of per-handle allocations.
+// Some callers cannot call cudaMalloc.  A framework whose caching allocator
+// owns (nearly) all device memory leaves no room for allocations made behind
+// its back, and every cudaFree synchronises the whole device.  A fitter that
+// evaluates thousands of parameter points per second cannot take that
+// synchronisation inside its loop.  A plugin that a host application hands
+// only device pointers and a stream is not allowed to own device memory at
+// all.  For such callers this entry point runs the single-grid calculation
+// (precompute, then propagation) on the caller's device pointers and stream,
+// with its scratch tables in a file-scope __device__ array instead of
+// per-handle allocations.
 //
 // The array is sized for grids up to kNoAllocMaxCosines x kNoAllocMaxEnergies
 // and kNoAllocMaxRows density rows, in either precision (about 14 MB); every
-// GPU that loads the library holds it until the process exits.  All calls on
-// one device share it: every region is rewritten before it is read, so no call
-// depends on a previous one, but calls whose work overlaps on the GPU (other
-// streams, other host threads) race on it and must be serialised by the caller.
+// GPU that loads the library holds it until the process exits.  The first call
+// on a device sets that device up (the array's device address, and the two
+// phase tables, written once from the same host function the handle path
+// uses, so both paths compute with the same bits).  Every later call rewrites
+// each region it reads, so no call depends on the previous one's data; calls
+// whose work overlaps on the GPU (other streams, other host threads) race on
+// the array and must be serialised by the caller.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <mutex>
 #include <string>
@@ -39,9 +45,17 @@ constexpr size_t kNaTab = align256((size_t)kNoAllocMaxEnergies * kNoAllocMaxLaye
 constexpr size_t kNaPe = align256((size_t)kPerEWords * kNoAllocMaxEnergies * 8);
 constexpr size_t kNaLen = align256((size_t)kNoAllocMaxCosines * kNoAllocLayersPad * 8);
 constexpr size_t kNaMaxl = align256((size_t)kNoAllocMaxCosines * 4);
-constexpr size_t kNaPhase = align256((size_t)kPhaseTabBytes);
+constexpr size_t kNaPhase = align256((size_t)kPhaseTabBytes);  // one table per precision
 constexpr size_t kNaBody = align256((size_t)2 * kNoAllocMaxLayers * 8);  // radii, rho*Ye
-constexpr size_t kNaBytes = kNaTab + kNaPe + kNaLen + kNaMaxl + kNaPhase + kNaBody;
+constexpr size_t kNaBytes = kNaTab + kNaPe + kNaLen + kNaMaxl + 2 * kNaPhase + kNaBody;
+
+// offsets of the regions in the array
+constexpr size_t kOffPe = kNaTab;
+constexpr size_t kOffLen = kOffPe + kNaPe;
+constexpr size_t kOffMaxl = kOffLen + kNaLen;
+constexpr size_t kOffPhaseMixed = kOffMaxl + kNaMaxl;  // written once per device at set-up
+constexpr size_t kOffPhaseFp64 = kOffPhaseMixed + kNaPhase;  // written once per device at set-up
+constexpr size_t kOffBody = kOffPhaseFp64 + kNaPhase;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
 
@@ -52,23 +66,13 @@ struct NoAllocBody {
     double coslimit[kNoAllocMaxRows];   // propagator.hpp:149-158
 };
 
-// Writes the layer radii and densities, the Q1.30/float cos-sin table and the
-// layer count of every cosine (propagator.hpp:301-307) into the scratch.
+// Writes the layer radii and densities and the layer count of every cosine
+// (propagator.hpp:301-307) into the scratch.
 __global__ void noalloc_setup_kernel(NoAllocBody body, const double* cosines, int n_cos, double* radii,
-                                     double* rhoye, int4* ptab, int* maxl, int mixed) {
+                                     double* rhoye, int* maxl) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < body.n) radii[t] = body.radii[t];
     if (t <= body.n) rhoye[t] = body.rhoye[t];
-    if (t <= kPhaseTabN) {
-        double s, c;
-        sincospi((double)(t - kPhaseTabN / 2) / (kPhaseTabN / 2), &s, &c);
-        if (mixed)
-            ptab[t] = make_int4((int)__double2ll_rn(c * 1073741824.0), (int)__double2ll_rn(s * 1073741824.0),
-                                __float_as_int(__double2float_rn(c) * 1073741824.0f),
-                                __float_as_int(__double2float_rn(s) * 1073741824.0f));
-        else
-            ((double2*)ptab)[t] = make_double2(c, s);
-    }
     if (t < n_cos) {
         const double cz = cosines[t];
         int cnt = 0;
@@ -82,11 +86,30 @@ __global__ void noalloc_setup_kernel(NoAllocBody body, const double* cosines, in
 namespace {
 
 std::mutex g_noalloc_mutex;
-void* g_noalloc_ptr[256] = {};
+void* g_noalloc_ptr[256] = {};  // device address of the array, per device id; null until set up
 
 int nfail(int code, const std::string& m) {
     cp3::set_last_error(m);
     return code;
+}
+
+// Set-up of the current device `dev` (called under g_noalloc_mutex): the
+// device address of the scratch array -- its host-side name is only a
+// stand-in and must never be passed to a kernel -- and the phase tables of
+// both precisions, filled by the same host function as a handle's table and
+// copied once (synchronously) into their regions.
+cudaError_t noalloc_setup_device(int dev) {
+    void* base = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&base, cp3::g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    int4 tab[cp3::kPhaseTabN + 1];
+    unsigned char* sc = (unsigned char*)base;
+    cp3::fill_phase_table(true, tab);
+    if ((e = cudaMemcpy(sc + cp3::kOffPhaseMixed, tab, sizeof tab, cudaMemcpyHostToDevice)) != cudaSuccess) return e;
+    cp3::fill_phase_table(false, tab);
+    if ((e = cudaMemcpy(sc + cp3::kOffPhaseFp64, tab, sizeof tab, cudaMemcpyHostToDevice)) != cudaSuccess) return e;
+    g_noalloc_ptr[dev] = base;
+    return cudaSuccess;
 }
 
 }  // namespace
@@ -113,32 +136,20 @@ extern "C" int cp3_propagate_noalloc(int precision, int type, const double* d_co
     const double par[7] = {theta12, theta13, theta23, dcp, dm12sq, dm23sq, height_km};
     for (double v : par)
         if (!std::isfinite(v)) return nfail(CP3_ERR_ARGUMENT, "propagate_noalloc: parameters must be finite");
-    // setDensity (propagator.hpp:117-161): one monotone order, outside-in
+    // setDensity (propagator.hpp:117-161), the same checks and order as cp3_set_density
+    BodyRow rows[kNoAllocMaxRows];
+    if (const char* msg = order_body(radii, rhos, ye, n_rows, rows)) return nfail(CP3_ERR_ARGUMENT, msg);
     NoAllocBody body{};
     body.n = n_rows;
-    bool flip = false;
-    if (n_rows >= 2) {
-        const int sign = (radii[1] - radii[0] > 0 ? 1 : -1);
-        for (int i = 1; i < n_rows; i++)
-            if ((radii[i] - radii[i - 1]) * sign < 0) return nfail(CP3_ERR_ARGUMENT, "radii order messed up");
-        flip = sign == 1;
-    }
     body.rhoye[0] = 0.0;
     for (int i = 0; i < n_rows; i++) {
-        const int s = flip ? n_rows - 1 - i : i;
-        const double y = ye ? ye[s] : 0.5;
-        if (!(radii[s] >= 0.0) || !(rhos[s] >= 0.0) || !(y >= 0.0 && y <= 1.0))
-            return nfail(CP3_ERR_ARGUMENT, "setDensity : bad radius, density or electron fraction");
-        body.radii[i] = radii[s];
-        body.rhoye[i + 1] = rhos[s] * y;
-        double x = -1 * std::sqrt(1 - (body.radii[i] * body.radii[i] / (kREarth * kREarth)));
-        if (i == 0) x = 0;
-        body.coslimit[i] = x;
+        body.radii[i] = rows[i].radius;
+        body.rhoye[i + 1] = rows[i].rho * rows[i].ye;
+        body.coslimit[i] = rows[i].coslimit;
     }
     if (n_cosines == 0 || n_energies == 0) return CP3_OK;
 
-    // set-up once per device, with that device current: the device address of
-    // the scratch array (its host-side name is not a device address)
+    // set-up once per device, with that device current
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return nfail(CP3_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
@@ -146,35 +157,31 @@ extern "C" int cp3_propagate_noalloc(int precision, int type, const double* d_co
     void* base = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-        if (!g_noalloc_ptr[dev]) {
-            e = cudaGetSymbolAddress(&g_noalloc_ptr[dev], g_noalloc_scratch);
-            if (e != cudaSuccess) {
-                g_noalloc_ptr[dev] = nullptr;
-                return nfail(CP3_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-            }
-        }
+        if (!g_noalloc_ptr[dev] && (e = noalloc_setup_device(dev)) != cudaSuccess)
+            return nfail(CP3_ERR_CUDA, std::string("propagate_noalloc set-up: ") + cudaGetErrorString(e));
         base = g_noalloc_ptr[dev];
     }
+    const bool mixed = precision == CP3_PRECISION_MIXED;
     unsigned char* sc = (unsigned char*)base;
     void* tab = sc;
-    void* pe = sc + kNaTab;
-    void* len = sc + kNaTab + kNaPe;
-    int* maxl = (int*)(sc + kNaTab + kNaPe + kNaLen);
-    int4* ptab = (int4*)(sc + kNaTab + kNaPe + kNaLen + kNaMaxl);
-    double* d_radii = (double*)(sc + kNaTab + kNaPe + kNaLen + kNaMaxl + kNaPhase);
+    void* pe = sc + kOffPe;
+    void* len = sc + kOffLen;
+    int* maxl = (int*)(sc + kOffMaxl);
+    const int4* ptab = (const int4*)(sc + (mixed ? kOffPhaseMixed : kOffPhaseFp64));
+    double* d_radii = (double*)(sc + kOffBody);
     double* d_rhoye = d_radii + kNoAllocMaxLayers;
 
-    const bool mixed = precision == CP3_PRECISION_MIXED;
     cudaStream_t s = (cudaStream_t)stream;
     cudaGetLastError();  // an earlier failed call must not be reported by the checks below
     const int nl = n_rows + 1;
     const int nl_pad = (nl + 1) / 2 * 2;
+    // the default launch shape of a handle (cp3_create), so that both paths
+    // run the same kernels on the same tiles
     const int te = 64, groups = mixed ? 4 : 2, cchunk = 32;
     const int n_en_pad = (n_energies + te - 1) / te * te;
     {
-        const int n = std::max(n_cosines, kPhaseTabN + 1);
-        noalloc_setup_kernel<<<(n + 255) / 256, 256, 0, s>>>(body, d_cosines, n_cosines, d_radii, d_rhoye, ptab,
-                                                             maxl, precision == CP3_PRECISION_MIXED ? 1 : 0);
+        const int n = std::max(n_cosines, n_rows + 1);
+        noalloc_setup_kernel<<<(n + 255) / 256, 256, 0, s>>>(body, d_cosines, n_cosines, d_radii, d_rhoye, maxl);
         if ((e = cudaGetLastError()) != cudaSuccess)
             return nfail(CP3_ERR_CUDA, std::string("setup kernel: ") + cudaGetErrorString(e));
     }
@@ -190,6 +197,7 @@ extern "C" int cp3_propagate_noalloc(int precision, int type, const double* d_co
     pa.pb.maxlayers = maxl;
     pa.pb.radii = d_radii;
     pa.pb.rhoye = d_rhoye;
+    // a handle's height after setProductionHeight (propagator.hpp:279-286)
     pa.pb.height_cm = height_km * 100000.0;
     fill_osc_params(pa.osc, theta12, theta13, theta23, dcp, dm12sq, dm23sq, type == CP3_ANTINEUTRINO);
     pa.tab = tab;

@@ -219,17 +219,6 @@ int cp3_get_maxlayers(cp3_propagator* p, int* out, int n);
 int cp3_set_kernel_timing(cp3_propagator* p, int enable);
 int cp3_last_kernel_ms(cp3_propagator* p, float* prep_ms, float* propagate_ms);
 
-/* Measured throughput of one GPU pipe on `device`, in operations per second
- * (no reference counterpart; it gives the roofline denominators):
- *   CP3_PIPE_IMAD_WIDE  32x32 -> 64 integer products (mul.wide.s32), the
- *                       Q1.30 chain's multiply
- *   CP3_PIPE_FFMA       FP32 fused multiply-add
- *   CP3_PIPE_DFMA       FP64 fused multiply-add                                */
-#define CP3_PIPE_IMAD_WIDE 0
-#define CP3_PIPE_FFMA 1
-#define CP3_PIPE_DFMA 2
-int cp3_pipe_peak(int device, int pipe, double* ops_per_second);
-
 /* ------------------------------------------------------------------ batches
  * Many independent propagations ("parameter sets") evaluated together: set s
  * has its own oscillation parameters, density scale and grid of
@@ -299,29 +288,44 @@ int cp3_loglik_set_observed(cp3_loglik* L, const double* counts);
  * grad (may be NULL) receives 6 + n_rows values. */
 int cp3_loglik_evaluate(cp3_loglik* L, int type, const double* params, const double* rhos,
                         double* loglik, double* grad);
+/* Record CUDA events around each of the evaluation's three kernels (prep,
+ * pair, layer) from the next evaluation on (0 disables; toggling recaptures
+ * the evaluation graph); cp3_loglik_last_kernel_ms returns the durations of
+ * the last evaluation. */
+int cp3_loglik_set_kernel_timing(cp3_loglik* L, int enable);
+int cp3_loglik_last_kernel_ms(cp3_loglik* L, float* prep_ms, float* pair_ms, float* layer_ms);
 
 /* ------------------------------------------------------------- no allocation
- * One calculation that allocates nothing, for callers that cannot call
- * cudaMalloc: code running while a stream is captured into a CUDA graph,
- * callers whose framework allocator must own all device memory, and
- * latency-bound loops that cannot take the device synchronisation of
- * cudaMalloc/cudaFree.  No counterpart in the reference (its
- * CudaPropagatorSingle allocates in its constructor, cudapropagator.cuh:73-79).
+ * One calculation that allocates nothing.  No counterpart in the reference.
+ * It is for callers that cannot call cudaMalloc:
+ *   - code inside a framework whose caching allocator owns (nearly) all device
+ *     memory, so that an allocation behind its back can fail, and whose
+ *     cudaFree would synchronise the whole device;
+ *   - fitters evaluating thousands of parameter points per second, which
+ *     cannot take that synchronisation inside their loop;
+ *   - plugins that a host application hands only device pointers and a
+ *     stream, and that may not own device memory.
  *
  * Runs on the current device and `stream` (NULL: the default stream).  Inputs
  * d_cosines[n_cosines] and d_energies[n_energies] and the output
  * d_out[9][n_cosines][n_energies] (float for CP3_PRECISION_MIXED, double for
  * CP3_PRECISION_FP64, plane in*3+out as cp3_result_device_ptr) are device
  * memory owned by the caller; radii/rhos/ye (ye may be NULL: 0.5) are host
- * arrays read during the call, with the semantics of cp3_set_density.  Results
- * equal those of cp3_create ... cp3_calculate_probabilities on the same inputs.
+ * arrays read during the call, with the checks and messages of
+ * cp3_set_density.  The results are bit for bit those of cp3_create,
+ * cp3_set_* and cp3_calculate_probabilities with the default launch shape on
+ * the same inputs (production height set after the cosine list).
  * Scratch lives in one static device array sized for the limits below (about
- * 14 MB, held by every GPU that loads the library until exit); larger problems
- * are rejected with CP3_ERR_LIMIT.  The first call on a device looks up that
- * array's device address (cudaGetSymbolAddress), so make it before any stream
- * capture.  Calls share the array: calls whose work overlaps on the GPU race
- * and must be serialised by the caller.  The call is asynchronous with respect
- * to the host. */
+ * 14 MB, held by every GPU that loads the library until the process exits);
+ * larger problems are rejected with CP3_ERR_LIMIT, and nothing is allocated
+ * (no cudaMalloc, cudaFree or allocating library call).  The first call on a
+ * device sets that device up: it looks up the array's device address
+ * (cudaGetSymbolAddress) and copies the phase tables into it synchronously,
+ * so make that first call before any stream capture.  Every call shares the
+ * array, which keeps the last call's contents; each call rewrites what it
+ * reads before reading it, but calls whose work overlaps on the GPU (other
+ * streams or host threads) race on it and must be serialised by the caller.
+ * After the set-up the call is asynchronous with respect to the host. */
 #define CP3_NOALLOC_MAX_COSINES 8192
 #define CP3_NOALLOC_MAX_ENERGIES 8192
 #define CP3_NOALLOC_MAX_ROWS 15

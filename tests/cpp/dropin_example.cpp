@@ -3,8 +3,12 @@
 // libcudaprob3_gb300.so.  Writes raw doubles to argv[1], per propagator: its
 // cosine grid, its energy grid, then [cosine][energy][9] probabilities, for
 //   CudaPropagatorSingle<double>, CudaPropagatorSingle<float>,
-//   CudaPropagator<double>({0, 0}) and CudaPropagator<float>({0}).
-// The grid, body and parameters are fixed; the test compares with the oracle.
+//   CudaPropagator<double>({0, 0}), CudaPropagator<float>({0}),
+//   CudaPropagator<double>({0}) and CudaPropagator<double>({0, 0, 0}).
+// The 37 cosines are dealt cyclically over 2 or 3 parts (not a multiple of
+// either), so getProbability's routing to (part, local index) is checked on
+// uneven parts.  The grid, body and parameters are fixed; the test compares
+// with the oracle.
 #include <cmath>
 #include <cstdio>
 #include <memory>
@@ -72,6 +76,10 @@ int main(int argc, char** argv) {
         run(c.get(), nc, ne, argv[2], out);
         std::unique_ptr<Propagator<float>> d(new CudaPropagator<float>(std::vector<int>{0}, nc, ne));
         run(d.get(), nc, ne, argv[2], out);
+        std::unique_ptr<Propagator<double>> f(new CudaPropagator<double>(std::vector<int>{0}, nc, ne));
+        run(f.get(), nc, ne, argv[2], out);
+        std::unique_ptr<Propagator<double>> g(new CudaPropagator<double>(std::vector<int>{0, 0, 0}, nc, ne));
+        run(g.get(), nc, ne, argv[2], out);
         // the reference's ordering rule and index check throw std::runtime_error
         bool threw = false;
         try {

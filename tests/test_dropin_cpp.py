@@ -49,9 +49,12 @@ def test_cpp_dropin_runs_like_reference_example(gpu):
         assert r.returncode == 0, r.stderr
         raw = np.fromfile(out, dtype=np.float64)
     per = nc + ne + nc * ne * 9
-    assert raw.size == 4 * per
+    assert raw.size == 6 * per
     B = G.PREM_12
-    for k, (tol, f32) in enumerate(((1e-11, False), (1e-6, True), (1e-11, False), (1e-6, True))):
+    # Single<double>, Single<float>, CudaPropagator<double>({0,0}), <float>({0}),
+    # <double>({0}), <double>({0,0,0})
+    kinds = ((1e-11, False), (1e-6, True), (1e-11, False), (1e-6, True), (1e-11, False), (1e-11, False))
+    for k, (tol, f32) in enumerate(kinds):
         blk = raw[k * per:(k + 1) * per]
         c, e = blk[:nc], blk[nc:nc + ne]
         got = blk[nc + ne:].reshape(nc, ne, 9)

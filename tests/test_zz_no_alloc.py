@@ -1,13 +1,16 @@
 """The entry point that allocates nothing, cp3_propagate_noalloc, against the
 regular handle path (cp3_create ... cp3_calculate_probabilities).
 
-It serves callers that cannot call cudaMalloc: code running while a stream is
-captured into a CUDA graph, callers whose allocator must own all device memory,
-and loops that cannot take the synchronisation of cudaMalloc/cudaFree.  Its
-scratch is one static device array, shared by all calls, so two calls in a row
-with different grids, bodies and neutrino types check that nothing carries
-over from one call to the next.  This file is collected last so that a run
-that stops at the first failure has run every other test first.
+It serves callers that cannot call cudaMalloc: code inside a framework whose
+caching allocator owns nearly all device memory (an allocation behind its back
+can fail, and cudaFree synchronises the device), fitters that evaluate many
+parameter points per second and cannot take that synchronisation in their
+loop, and plugins handed only device pointers and a stream.  Its scratch is
+one static device array shared by all calls, so two calls in a row with
+different grids, bodies and neutrino types check that nothing carries over
+from one call to the next.  Both paths build the same tables with the same
+code, so their planes must be equal bit for bit.  This file is collected last
+so that a run that stops at the first failure has run every other test first.
 """
 import ctypes
 
@@ -19,7 +22,6 @@ from cudaprob3_gb300 import grids as G
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp64": 1e-11, "mixed": 1e-6}  # the tolerances of the parity tests
 CODE = {"fp64": _lib.PRECISION_FP64, "mixed": _lib.PRECISION_MIXED}
 
 
@@ -64,7 +66,7 @@ def test_noalloc_matches_handle_path_twice(gpu, precision):
     for cos, en, body, params, anti in calls:
         got = noalloc_path(torch, precision, cos, en, body, params, anti)
         want = handle_path(gpu, precision, cos, en, body, params, anti)
-        assert np.abs(got - want).max() <= TOL[precision]
+        assert np.array_equal(got, want), "max |dP| %.3g" % np.abs(got - want).max()
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch(gpu):
@@ -81,3 +83,12 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(gpu):
     rc = lib.cp3_propagate_noalloc(1, 0, ctypes.c_void_p(16), 16, ctypes.c_void_p(16), 16, dp(r16), dp(d16), None,
                                    16, *args, ctypes.c_void_p(16), None)
     assert rc == _lib.ERR_LIMIT and b"rows" in lib.cp3_last_error()
+    # non-finite radii and densities are refused like cp3_set_density refuses them
+    for bad_r, bad_d in ((np.inf, 4.0), (6371.0, np.inf), (np.nan, 4.0)):
+        rb = r.copy()
+        db = d.copy()
+        rb[-1] = bad_r
+        db[-1] = bad_d
+        rc = lib.cp3_propagate_noalloc(1, 0, ctypes.c_void_p(16), 16, ctypes.c_void_p(16), 16, dp(rb), dp(db), None,
+                                       int(rb.size), *args, ctypes.c_void_p(16), None)
+        assert rc == _lib.ERR_ARGUMENT and b"finite" in lib.cp3_last_error()
