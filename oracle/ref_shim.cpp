@@ -48,7 +48,37 @@ static int run(int nc, const T* cosv, int ne, const T* ev, int nr, const T* r, c
     return 0;
 }
 
+// The same with the body read by the reference's own setDensityFromFile
+// (propagator.hpp:169-184) from `path`.
+template <class T>
+static int run_file(int nc, const T* cosv, int ne, const T* ev, const char* path, T t12, T t13, T t23, T dcp,
+                    T dm12, T dm23, T h, int anti, int threads, T* out) {
+    try {
+        cudaprob3::CpuPropagator<T> p(nc, ne, threads);
+        p.setEnergyList(std::vector<T>(ev, ev + ne));
+        p.setCosineList(std::vector<T>(cosv, cosv + nc));
+        p.setMNSMatrix(t12, t13, t23, dcp);
+        p.setNeutrinoMasses(dm12, dm23);
+        p.setDensityFromFile(std::string(path));
+        p.setProductionHeight(h);
+        p.calculateProbabilities(anti ? cudaprob3::Antineutrino : cudaprob3::Neutrino);
+        for (int ic = 0; ic < nc; ic++)
+            for (int ie = 0; ie < ne; ie++)
+                for (int t = 0; t < 9; t++)
+                    out[(size_t(ic) * ne + ie) * 9 + t] = p.getProbability(ic, ie, cudaprob3::ProbType(t));
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return -1;
+    }
+    return 0;
+}
+
 extern "C" {
+int ref_calculate_file_f64(int nc, const double* c, int ne, const double* e, const char* path, double t12,
+                           double t13, double t23, double dcp, double dm12, double dm23, double h, int anti,
+                           int threads, double* out) {
+    return run_file<double>(nc, c, ne, e, path, t12, t13, t23, dcp, dm12, dm23, h, anti, threads, out);
+}
 int ref_calculate_f64(int nc, const double* c, int ne, const double* e, int nr, const double* r,
                       const double* rho, double t12, double t13, double t23, double dcp,
                       double dm12, double dm23, double h, int anti, int threads, double* out) {

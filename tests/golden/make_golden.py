@@ -6,10 +6,11 @@ stores inputs plus outputs as .npz.  It needs the reference sources, so it runs
 only on the machine that has them; the fixtures it writes are committed and the
 tests read those.
 
-    python tests/golden/make_golden.py [--ref-dir DIR]
+    REF_DIR=<reference source directory> python tests/golden/make_golden.py
 """
 import argparse
 import os
+import shutil
 import sys
 
 import numpy as np
@@ -46,8 +47,11 @@ def case(name, cos, en, radii, rhos, ye, params, height=22.0, anti=False, kc=Non
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-dir", default="/root/reference")
+    ap.add_argument("--ref-dir", default=os.environ.get("REF_DIR"),
+                    help="the reference's source directory (default: $REF_DIR)")
     a = ap.parse_args()
+    if not a.ref_dir:
+        sys.exit("set REF_DIR (or --ref-dir) to the reference's source directory")
     oracle.build(a.ref_dir)
     if not oracle.ref_available():
         sys.exit("reference library not built; fixtures need the reference sources")
@@ -100,6 +104,48 @@ def main():
         r59, d59 = G.read_density_file(mpath)
         case("prem59", G.linspace(-1, 0, 64), G.logspace(0.1, 1000, 48), r59, d59,
              np.where(r59 <= 3480.0, 0.468, 0.497), nom, note="59-row PREM table")
+    density_files(a.ref_dir)
+
+
+# the density models shipped with the reference (example/models), copied as
+# fixtures, and two variants of the 12-layer file for the edge cases of the
+# two-column read loop (propagator.hpp:169-184)
+MODELS = ("PREM_4layer.dat", "PREM_10layer.dat", "PREM_12layer.dat", "PREM_59layer.dat")
+MODELS_DIR = os.path.join(HERE, "models")
+
+
+def density_files(ref_dir):
+    """Goldens of the reference's setDensityFromFile on each model file, on the
+    grid of tests/cpp/dropin_example.cpp (37 cosines in [-1, 0] x 45 energies
+    over 0.5-100 GeV, nominal parameters, neutrinos): the rows the reference
+    reads are stored as radii/rhos (ye 0.5, its fixed factor), so the files
+    also serve the setDensity path."""
+    os.makedirs(MODELS_DIR, exist_ok=True)
+    for m in MODELS:
+        shutil.copyfile(os.path.join(ref_dir, "example", "models", m), os.path.join(MODELS_DIR, m))
+    with open(os.path.join(MODELS_DIR, "PREM_12layer.dat")) as f:
+        rows = f.read().splitlines()
+    # trailing blank lines and spaces: skipped by the stream extraction
+    with open(os.path.join(MODELS_DIR, "PREM_12layer_trailing_blank.dat"), "w") as f:
+        f.write("\n".join(rows) + "\n\n   \n\n")
+    # the rows outside-in (setDensity accepts either order) with a text row
+    # after the eighth: the read loop stops there, so the body is the eight
+    # outermost rows (no radius-0 row: the innermost is crossed as a full chord)
+    desc = [r for r in rows if r.strip()][::-1]
+    with open(os.path.join(MODELS_DIR, "PREM_12layer_stops_at_text.dat"), "w") as f:
+        f.write("\n".join(desc[:8] + ["end of the mantle rows"] + desc[8:]) + "\n")
+    c, e = G.linspace(-1.0, 0.0, 37), G.logspace(0.5, 100.0, 45)
+    for name in sorted(os.listdir(MODELS_DIR)):
+        path = os.path.join(MODELS_DIR, name)
+        radii, rhos = G.read_density_file(path)
+        probs = oracle.ref_calculate_file(c, e, path, G.NOMINAL, 22.0, False)
+        out = os.path.join(HERE, "file_" + name[:-4] + ".npz")
+        np.savez_compressed(out, cosines=c, energies=e, radii=radii, rhos=rhos, ye=np.full(radii.size, 0.5),
+                            params=np.asarray(G.NOMINAL, np.float64), height_km=np.float64(22.0),
+                            anti=np.int32(0), idx_c=np.arange(c.size), idx_e=np.arange(e.size), probs=probs,
+                            density_file=np.str_(name),
+                            note=np.str_("the reference's setDensityFromFile on models/" + name))
+        print("%-40s %2d rows -> %d pairs stored" % (os.path.basename(out), radii.size, c.size * e.size))
 
 
 if __name__ == "__main__":
