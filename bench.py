@@ -49,11 +49,20 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="target CPU time of the baseline sample")
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--precision-sets", type=int, default=64,
+                    help="parameter sets of the 8192 x 8192 precision table in the default line (0: skip)")
     ap.add_argument("--workload", choices=["grid4096", "batch", "precision", "gradient", "rates", "heights"],
                     default="grid4096",
                     help="grid4096: the headline line; batch: 1024 parameter sets with uneven grids in one "
                          "graph launch; precision: 64 parameter sets on the 8192 x 8192 grid")
     ap.add_argument("--sets", type=int, default=0, help="number of parameter sets (batch/precision)")
+    # one small case for profilers (ncu): no timing contract, no JSON line
+    ap.add_argument("--profile-case", choices=["planes", "rates", "heights", "gradient"], default=None,
+                    help="run one square grid (or the gradient evaluation) for a profiler instead of a benchmark")
+    ap.add_argument("--n", type=int, default=2048, help="profile case: cosines = energies")
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed", help="profile case: arithmetic")
+    ap.add_argument("--repeat", type=int, default=1, help="profile case: calculations")
+    ap.add_argument("--anti", action="store_true", help="profile case: antineutrinos")
     return ap.parse_args()
 
 
@@ -113,6 +122,61 @@ def survey_flops_per_pair(M):
     M = np.asarray(M, dtype=np.int64)
     nmm = np.where(M >= 1, 2 * M, 1)
     return (M + 1) * 222 + nmm * 216 + 27
+
+
+def ll_pair_products_per_pair(M):
+    """Real multiply-adds of one (cosine, energy) bin in ll_pair_kernel
+    (cp3_loglik.cu): the forward chain (D_0 Gamma', T_0, the inner steps
+    U = D_l Y, Y = T_l U, G = Y^T D_M Y, G X', the 2x2 block, |B|^2) plus the
+    adjoint (the seeds, the adjoints of X, Lambda', G, x, T_0, Gamma', D_0,
+    Y and D_M, and per crossed shell the un-multiplied chain and its
+    adjoint), every complex product counted as four real ones and every real
+    times complex as two; phase evaluations and warp sums are not counted.
+    For M >= 2 crossed shells: 400 + 90 (M - 2) forward and 874 + 278 (M - 2)
+    backward."""
+    M = np.asarray(M, dtype=np.int64)
+    return np.where(M >= 2, 1274 + 368 * (M - 2), np.where(M == 1, 1086, 178))
+
+
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one
+# propagate_kernel<mixed> launch per pair, from one ncu capture of the
+# 4096 x 4096 launch, and the SHA-256 of the device sources the kernel was
+# compiled from at that capture.  When the sources differ the figure no longer
+# describes the kernel, and the roofline's traffic is reported as null.
+TRAFFIC_BYTES_PER_PAIR = 547_799_552 / (4096 * 4096)
+TRAFFIC_SOURCES_SHA = "c19b726b7be8342e5f74ccaccda0114d3a6c83aeffddbbc79acdedb78aec6253"
+TRAFFIC_SOURCES = ("cp3_arith.cuh", "cp3_chain.cuh", "cp3_internal.h", "cp3_physics.cuh", "cp3_tile.cuh")
+
+
+def traffic_sources_sha():
+    """SHA-256 over the device sources of the propagate kernel's body."""
+    import hashlib
+    h = hashlib.sha256()
+    for name in TRAFFIC_SOURCES:
+        with open(os.path.join(ROOT, "cudaprob3_gb300", "csrc", name), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()
+
+
+# ------------------------------------------------------------- pipe peaks --
+def pipe_peak(pipe, device):
+    """(operations/s, SM MHz during the probe, SM count) of one pipe -- 0
+    mul.wide.s32 integer products, 1 FP32 FMA, 2 FP64 FMA -- from the
+    benchmark's own probe library (bench_pipes.cu, built by build())."""
+    import ctypes
+    path = os.path.join(ROOT, "libbench_pipes.so")
+    lib = ctypes.CDLL(path)
+    lib.bench_pipe_peak.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                    ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
+    lib.bench_pipe_peak.restype = ctypes.c_int
+    ops, mhz, sms = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+    rc = lib.bench_pipe_peak(int(device), int(pipe), ctypes.byref(ops), ctypes.byref(mhz), ctypes.byref(sms))
+    if rc != 0:
+        raise RuntimeError("pipe probe failed with CUDA error %d" % rc)
+    return ops.value, mhz.value, sms.value
+
+
+PIPE_IMAD_WIDE, PIPE_FFMA, PIPE_DFMA = 0, 1, 2
 
 
 # ------------------------------------------------------------------ clocks --
@@ -219,6 +283,51 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------- the reference's kernel --
+def reference_gpu_leg(value, fp64_value):
+    """The reference's own CUDA kernel, calculateKernel<double> and <float>
+    (physics.hpp:705-721), recompiled for sm_103a, launched as
+    CudaPropagatorSingle launches it (64-thread blocks) on the same 4096 x 4096
+    grid, body and parameters as the headline, nu and nubar, with the constants
+    and device arrays its own host code prepared (oracle/ref_gpu_kernel.cu,
+    ref_gpu_inputs.cpp, ref_gpu_driver.cpp): per type the median of 5 timed
+    launches (CUDA events) after one warm-up; outputs (1.2 GB / 0.6 GB per
+    launch) exceed L2.  Errors against the oracle on every 32nd cosine and
+    energy; the float kernel gets the grid and body rounded to float."""
+    import oracle
+    status = oracle.ref_gpu_status()
+    if status:
+        return {"unavailable": status}
+    cos, en, B, nom = grid()
+    idx = np.arange(0, NC, 32)
+    want = {anti: oracle.calculate(cos[idx], en[idx], B.radii, B.rho_eff(), nom, 22.0, anti) for anti in (False, True)}
+    out = {"workload": WORKLOAD, "launch": "calculateKernel<T>, 64-thread blocks, ceil(nE/64)*nC blocks, one launch "
+                                          "per neutrino type (cudapropagator.cuh:191-220)",
+           "timing": "median of 5 launches per type after a warm-up, CUDA events; step = nu + nubar"}
+    try:
+        for prec, name in (("f64", "double"), ("f32", "float")):
+            ms = 0.0
+            err = 0.0
+            mean = 0.0
+            rec = None
+            for anti in (False, True):
+                rec, sub = oracle.ref_gpu_run(prec, anti, reps=5, stride=32)
+                ms += rec["median_ms"]
+                d = np.abs(sub - want[anti])
+                err = max(err, float(d.max()))
+                mean += float(d.mean()) / 2
+            out[name] = {"pairs_per_s": 2 * NC * NE / (ms * 1e-3), "ms_per_step": ms,
+                         "max_abs_dp_vs_oracle_subset": err, "mean_abs_dp_vs_oracle_subset": mean,
+                         "registers": rec["registers"], "local_bytes_per_thread": rec["local_bytes"]}
+    except (RuntimeError, OSError, ValueError, KeyError) as exc:
+        return {"unavailable": "the reference kernel did not run: %s" % str(exc)[:300]}
+    out["mixed_speedup_vs_reference_double"] = value / out["double"]["pairs_per_s"]
+    out["mixed_speedup_vs_reference_float"] = value / out["float"]["pairs_per_s"]
+    if fp64_value:
+        out["fp64_speedup_vs_reference_double"] = fp64_value / out["double"]["pairs_per_s"]
+    return out
+
+
 # ------------------------------------------------------------------- ours --
 def make_prop(cp, precision, cos, en, B, nom, device):
     p = cp.CudaPropagatorSingle(device, len(cos), len(en), precision=precision)
@@ -277,8 +386,6 @@ def run_ours(args, world, rank, local):
     import torch
 
     import cudaprob3_gb300 as cp
-    from cudaprob3_gb300 import _lib
-    from cudaprob3_gb300.propagator import pipe_peak
 
     dev = local
     torch.cuda.set_device(dev)
@@ -362,9 +469,9 @@ def run_ours(args, world, rank, local):
     prop_ms = float(np.mean([k[1] for k in kt]))
     prep_ms = float(np.mean([k[0] for k in kt]))
     prods = float(products_per_pair(maxl).sum()) * NE
-    peak_prod = pipe_peak(_lib.PIPE_IMAD_WIDE, dev)
-    peak_ffma = pipe_peak(_lib.PIPE_FFMA, dev)
-    peak_dfma = pipe_peak(_lib.PIPE_DFMA, dev)
+    peak_prod, prod_mhz, n_sm = pipe_peak(PIPE_IMAD_WIDE, dev)
+    peak_ffma, _, _ = pipe_peak(PIPE_FFMA, dev)
+    peak_dfma, dfma_mhz, _ = pipe_peak(PIPE_DFMA, dev)
     out_bytes = 9 * NC * NE * 4
     survey_f = float(survey_flops_per_pair(maxl).sum()) * NE
     try:
@@ -372,16 +479,23 @@ def run_ours(args, world, rank, local):
         hbm_peak, hbm_src = float(mp["hbm_gbs"]), "MEASURED_PEAKS.json (measured)"
     except (OSError, KeyError, ValueError):
         hbm_peak, hbm_src = 6800.0, "fallback 6.8 TB/s"
-    # DRAM bytes (read + write) of one propagate_kernel<mixed> launch at
-    # 4096 x 4096 from an ncu capture of that launch (dram__bytes_read.sum +
-    # dram__bytes_write.sum; summary in profiles/propagate_mixed_4096x4096_ncu.md)
-    traffic = 547_799_552 if (NC, NE) == (4096, 4096) else None
+    # DRAM bytes of one launch: the captured per-pair figure times this
+    # launch's pairs, while the kernel's sources are those of the capture
+    sources_sha = traffic_sources_sha()
+    traffic_current = sources_sha == TRAFFIC_SOURCES_SHA
+    traffic = TRAFFIC_BYTES_PER_PAIR * NC * NE if traffic_current else None
     roofline = {
         "bound": "fma-pipe (mul.wide.s32 integer products on the FMA-heavy pipe)",
         "achieved": prods / (prop_ms * 1e-3) / 1e12, "peak": peak_prod / 1e12, "unit": "Tops/s",
         "frac": (prods / (prop_ms * 1e-3)) / peak_prod, "traffic": traffic,
         "kernel": "propagate_kernel<mixed>", "kernel_ms": prop_ms, "prep_kernel_ms": prep_ms,
-        "work_per_launch": prods, "peak_source": "measured live on this GPU (cp3_pipe_peak)",
+        "work_per_launch": prods,
+        "work_unit": "32x32->64 integer products, four-product form of every complex product (products_per_pair)",
+        "peak_source": "measured live on this GPU (bench_pipes.cu) at %.0f MHz SM clock, %d SMs" % (prod_mhz, n_sm),
+        "traffic_source": ("ncu capture of one 4096^2 launch (%.2f B/pair) x pairs of this launch; kernel sources "
+                           "unchanged since (sha %s)" % (TRAFFIC_BYTES_PER_PAIR, sources_sha[:12])) if traffic_current
+        else "null: the kernel's device sources changed since the last capture (sha %s)" % sources_sha[:12],
+        "algorithmic_out_bytes": out_bytes,
         "hbm_output_gbs": out_bytes / (prop_ms * 1e-3) / 1e9, "hbm_peak_gbs": hbm_peak,
         "hbm_frac": out_bytes / (prop_ms * 1e-3) / 1e9 / hbm_peak, "hbm_peak_source": hbm_src,
         "survey_equiv_tflops": survey_f / (prop_ms * 1e-3) / 1e12,
@@ -489,7 +603,8 @@ def run_ours(args, world, rank, local):
                              "note": "chain multiply-adds only; the FP64 phases (257-entry table and "
                                      "Taylor series, 15 FP64 instructions each) and the completion "
                                      "come on top",
-                             "peak_source": "measured live on this GPU (cp3_pipe_peak)"}}
+                             "peak_source": "measured live on this GPU (bench_pipes.cu) at %.0f MHz SM clock"
+                                            % dfma_mhz}}
         # precision of this step's mixed results against FP64 (every pair)
         for p, t in props:
             p.calculateProbabilitiesAsync(t)
@@ -517,6 +632,17 @@ def run_ours(args, world, rank, local):
         prec["mean_abs_dp_vs_oracle_subset"] = mean
         prec["oracle_subset"] = "every 32nd cosine x every 32nd energy (128 x 128), nu and nubar"
 
+    # the precision workload (8192 x 8192, parameter sets of seed 0): mixed
+    # against FP64 on every pair, both against the oracle on a subset
+    configs2 = None
+    if args.precision_sets > 0:
+        summary, per_set = precision_sets(dev, args.precision_sets)
+        configs2 = dict(summary, per_set=per_set)
+
+    reference_gpu = None
+    if rank == 0 and world == 1:
+        reference_gpu = reference_gpu_leg(value, fp64["value"] if fp64 else None)
+
     cpu = None
     configs0 = None
     if rank == 0 and world == 1:
@@ -540,7 +666,7 @@ def run_ours(args, world, rank, local):
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clocks, "fp64": fp64, "precision": prec,
             "speedup_vs_fp64": (value / fp64["value"]) if fp64 else None,
-            "configs0": configs0,
+            "configs0": configs0, "configs2_precision": configs2, "reference_gpu": reference_gpu,
         }
         print(json.dumps(line), flush=True)
     for p, _ in props:
@@ -616,6 +742,26 @@ def run_batch(args, world, rank, local):
         err = max(err, float(d.max()))
         errs.append(float(d.mean()))
     te, groups, cchunk, blocks = b.launch_shape()
+    # roofline: the four-product count of every pair of every set (its own
+    # grid and layer counts) over the whole graph's time -- the persistent
+    # propagate kernel shares that time with the co-running FP64 prep, so the
+    # fraction is a lower bound for the propagate kernel alone
+    ml = b.maxlayers()
+    ne_per_cos = np.repeat(np.asarray(ne, dtype=np.float64), np.asarray(nc, dtype=np.int64))
+    prods = float((products_per_pair(ml) * ne_per_cos).sum())
+    peak_prod, prod_mhz, n_sm = pipe_peak(PIPE_IMAD_WIDE, local)
+    roofline = {"bound": "fma-pipe (mul.wide.s32 integer products on the FMA-heavy pipe)",
+                "kernel": "batch_propagate_kernel<mixed> (persistent) with its graph",
+                "work_per_launch": prods,
+                "work_unit": "32x32->64 integer products, four-product form (products_per_pair) summed over every "
+                             "set's pairs",
+                "achieved": prods / (ms * 1e-3) / 1e12, "peak": peak_prod / 1e12, "unit": "Tops/s",
+                "frac": prods / (ms * 1e-3) / peak_prod, "traffic": None,
+                "time": "the whole graph launch (counter reset, 8 prep + 8 propagate launches), not the propagate "
+                        "kernel alone",
+                "peak_source": "measured live on this GPU (bench_pipes.cu) at %.0f MHz SM clock, %d SMs"
+                               % (prod_mhz, n_sm),
+                "hbm_output_gbs": pairs * 36 / (ms * 1e-3) / 1e9}
     if rank == 0:
         line = {"metric": "(cos,E) pairs/s, %d parameter sets with uneven grids in one persistent CUDA-graph "
                           "launch (mixed)" % n,
@@ -631,7 +777,7 @@ def run_batch(args, world, rank, local):
                            "autotune_s": tune_s, "autotune_best_ms": tune_ms},
                 "sequential": {"value": world * pairs / (seq_ms * 1e-3), "unit": "pairs/s", "ms_per_step": seq_ms,
                                "launches_per_step": 2 * n},
-                "speedup_vs_sequential": seq_ms / ms, "gpu_launches": 1 + 2 * args.steps,
+                "speedup_vs_sequential": seq_ms / ms, "gpu_launches": 1 + 2 * args.steps, "roofline": roofline,
                 "precision": {"max_abs_dp_vs_oracle_sampled_sets": err,
                               "mean_abs_dp_vs_oracle_sampled_sets": float(np.mean(errs)),
                               "sampled": "every %d-th set, every 16th cosine and energy" % max(1, n // 8)}}
@@ -832,16 +978,24 @@ def run_heights(args, world, rank, local):
         p.close()
 
 
-def run_precision(args, world, rank, local):
+PRECISION_N = 8192
+
+
+def precision_sets(local, nsets):
+    """The precision workload: nsets parameter sets of seed 0 (Gaussian around
+    nominal, random sign of dm32; neutrinos for even sets, antineutrinos for
+    odd ones) on the 8192 x 8192 grid (cosines in [-1, 0], 0.1-1000 GeV) of the
+    11-shell body.  Per set: the mixed and the FP64 kernel (CUDA events on
+    their stream), max/mean |dP| of mixed against FP64 over all 67M pairs
+    (on the device), and both against the oracle on every 128th cosine and
+    energy (64 x 64 pairs).  Returns the summary and the per-set rows."""
     import torch
 
     import cudaprob3_gb300 as cp
     from cudaprob3_gb300 import grids as G
     import oracle
 
-    torch.cuda.set_device(local)
-    n = 8192
-    nsets = args.sets or 64
+    n = PRECISION_N
     cos = G.linspace(-1.0, 0.0, n)
     en = G.logspace(0.1, 1000.0, n)
     B = G.PREM_12
@@ -874,33 +1028,51 @@ def run_precision(args, world, rank, local):
                 c.record(stream)
                 c.synchronize()
                 acc.append(a.elapsed_time(c))
-            d = (bm.double() - bf).abs()
+            d = (bm.double() - bf).abs_()
             dmax, dmean = float(d.max()), float(d.mean())
             del d
         want = oracle.calculate(cos[idx], en[idx], B.radii, B.rho_eff(), tuple(ps), 22.0, anti)
         gm = bm[:, idx][:, :, idx].double().cpu().numpy()
         gf = bf[:, idx][:, :, idx].cpu().numpy()
-        per_set.append({"set": k, "anti": anti, "max_vs_fp64": dmax, "mean_vs_fp64": dmean,
+        per_set.append({"set": k, "anti": anti, "dm32": float(ps[5]), "max_vs_fp64": dmax, "mean_vs_fp64": dmean,
                         "max_mixed_vs_oracle": float(np.abs(gm - want).max()),
+                        "mean_mixed_vs_oracle": float(np.abs(gm - want).mean()),
                         "max_fp64_vs_oracle": float(np.abs(gf - want).max())})
+    pm.close()
+    pf.close()
+    del bm, bf
+    torch.cuda.empty_cache()
     pairs = n * n
     mix_ms = float(np.median(tm))
     f64_ms = float(np.median(tf))
+    summary = {"workload": "8192 cos x 8192 E (0.1-1000 GeV), 11-shell PREM, %d parameter sets from seed 0 "
+                           "(nu for even sets, nubar for odd; %d with dm32 < 0)" % (nsets, sum(r["dm32"] < 0 for r in per_set)),
+               "oracle_subset": "every 128th cosine and energy (64 x 64) per set",
+               "max_mixed_vs_fp64": max(r["max_vs_fp64"] for r in per_set),
+               "max_of_set_means_mixed_vs_fp64": max(r["mean_vs_fp64"] for r in per_set),
+               "mean_of_set_means_mixed_vs_fp64": float(np.mean([r["mean_vs_fp64"] for r in per_set])),
+               "max_mixed_vs_oracle": max(r["max_mixed_vs_oracle"] for r in per_set),
+               "max_fp64_vs_oracle": max(r["max_fp64_vs_oracle"] for r in per_set),
+               "mixed_pairs_per_s": pairs / (mix_ms * 1e-3), "fp64_pairs_per_s": pairs / (f64_ms * 1e-3),
+               "mixed_ms_median": mix_ms, "fp64_ms_median": f64_ms, "speedup_mixed_vs_fp64": f64_ms / mix_ms,
+               "timing": "one calculation (prep + propagate) per set and form, CUDA events on its stream, median "
+                         "over the sets; outputs 2.4 GB (mixed) / 4.8 GB (FP64) per calculation exceed L2"}
+    return summary, per_set
+
+
+def run_precision(args, world, rank, local):
+    import torch
+
+    torch.cuda.set_device(local)
+    nsets = args.sets or 64
+    summary, per_set = precision_sets(local, nsets)
     if rank == 0:
         line = {"metric": "per-set max/mean |dP| of the mixed kernel, 8192 x 8192, %d parameter sets" % nsets,
-                "value": max(r["max_vs_fp64"] for r in per_set), "unit": "max |dP| mixed vs FP64 (all pairs)",
+                "value": summary["max_mixed_vs_fp64"], "unit": "max |dP| mixed vs FP64 (all pairs)",
                 "higher_is_better": False, "n_gpus": world, "data": "synthetic",
-                "config": {"workload": "8192 cos x 8192 E (0.1-1000 GeV), 11-shell PREM, %d sets from seed 0 "
-                                       "(nu for even sets, nubar for odd)" % nsets,
-                           "oracle_subset": "every 128th cosine and energy (64 x 64) per set"},
-                "mixed_pairs_per_s": pairs / (mix_ms * 1e-3), "fp64_pairs_per_s": pairs / (f64_ms * 1e-3),
-                "speedup": f64_ms / mix_ms, "mean_of_means_vs_fp64": float(np.mean([r["mean_vs_fp64"] for r in per_set])),
-                "max_mixed_vs_oracle": max(r["max_mixed_vs_oracle"] for r in per_set),
-                "max_fp64_vs_oracle": max(r["max_fp64_vs_oracle"] for r in per_set),
-                "per_set": per_set}
+                "config": {"workload": summary["workload"], "oracle_subset": summary["oracle_subset"]},
+                "summary": summary, "per_set": per_set}
         print(json.dumps(line), flush=True)
-    pm.close()
-    pf.close()
 
 
 def run_gradient(args, world, rank, local):
@@ -938,6 +1110,15 @@ def run_gradient(args, world, rank, local):
     fd_noise = np.where(steps > 0, 2.2e-16 * ll_abs / (2 * np.where(steps > 0, steps, 1.0)), 0.0)
     # components whose central difference is good to 1e-6 relative or better
     resolved = fd_noise < 1e-6 * np.abs(fd)
+    # layer counts of the bins (the library's own setDensity / maxlayers) and
+    # the pair kernel's multiply-adds over all bins
+    import cudaprob3_gb300 as cp
+    with cp.CudaPropagatorSingle(local, prob.cosines.size, 1, precision="fp64") as h:
+        h.setCosineList(prob.cosines)
+        h.setDensity(B.radii, B.rhos, B.ye)
+        ml = h.maxlayers()
+    pair_fmas = float(ll_pair_products_per_pair(ml).sum()) * prob.energies.size
+    peak = {"mixed": pipe_peak(PIPE_FFMA, local), "fp64": pipe_peak(PIPE_DFMA, local)}
     out = {}
     for precision in ("fp64", "mixed"):
         L = prob.make(device_id=local, precision=precision)
@@ -949,12 +1130,35 @@ def run_gradient(args, world, rank, local):
         for _ in range(n):
             ll, g = L.evaluate(prob.nominal, B.rhos)
         dt = (time.perf_counter() - t0) / n
+        # each kernel's time from events recorded inside the graph (a second,
+        # separately timed pass: the events are not part of the timed graph)
+        L.set_kernel_timing(True)
+        L.evaluate(prob.nominal, B.rhos)
+        kt = []
+        for _ in range(n):
+            L.evaluate(prob.nominal, B.rhos)
+            kt.append(L.last_kernel_ms())
+        L.set_kernel_timing(False)
+        prep_ms, pair_ms, layer_ms = (float(np.median([k[i] for k in kt])) for i in range(3))
+        pk, pk_mhz, pk_sms = peak[precision]
+        roof = {"bound": "FP32 FMA pipe" if precision == "mixed" else "FP64 pipe (DFMA)",
+                "kernel": "ll_pair_kernel<%s>" % ("float" if precision == "mixed" else "double"),
+                "work_per_launch": pair_fmas,
+                "work_unit": "real multiply-adds of the forward chain and its adjoint per bin "
+                             "(ll_pair_products_per_pair) summed over the 80,000 bins",
+                "kernel_ms": pair_ms, "achieved": pair_fmas / (pair_ms * 1e-3) / 1e12, "peak": pk / 1e12,
+                "unit": "T FMA/s", "frac": pair_fmas / (pair_ms * 1e-3) / pk, "traffic": None,
+                "peak_source": "measured live on this GPU (bench_pipes.cu) at %.0f MHz SM clock" % pk_mhz,
+                "kernels_ms": {"ll_prep_kernel": prep_ms, "ll_pair_kernel": pair_ms, "ll_layer_kernel": layer_ms},
+                "prep_and_layer": "FP64, latency-bound (a few warps per SM): %d eigen-solves per evaluation in "
+                                  "ll_prep_kernel, %d (energy, layer) back-propagations in ll_layer_kernel"
+                                  % (prob.energies.size * (B.rhos.size + 1), prob.energies.size * (B.rhos.size + 1))}
         names = list(PARAM_NAMES) + ["rho_row%d" % i for i in range(B.rhos.size)]
         rel = np.abs(g - fd) / np.linalg.norm(fd)
         # element-wise |g_k - fd_k| / |fd_k|; a zero FD component (the zero-width
         # centre row) is compared in absolute terms
         elem = np.where(fd != 0.0, np.abs(g - fd) / np.where(fd != 0.0, np.abs(fd), 1.0), np.abs(g))
-        out[precision] = {"evals_per_s": 1.0 / dt, "ms_per_eval": dt * 1e3, "loglik": ll,
+        out[precision] = {"evals_per_s": 1.0 / dt, "ms_per_eval": dt * 1e3, "loglik": ll, "roofline": roof,
                           "max_rel_grad_error": float(elem[resolved].max()),
                           "max_rel_grad_error_note": "element-wise |g - fd| / |fd| over the components whose "
                                                      "central difference carries less than 1e-6 relative "
@@ -972,6 +1176,7 @@ def run_gradient(args, world, rank, local):
                                        "(theta23, dcp, dm32); gradient w.r.t. 6 parameters + 12 row densities",
                            "wall_clock": "one evaluate() = graph launch with parameter upload and gradient "
                                          "download, host-timed"},
+                "roofline": out["mixed"]["roofline"],
                 "fp64": out["fp64"], "mixed": out["mixed"], "finite_differences": fd.tolist(),
                 "fd_noise_rel_per_param": {n_: float(v / abs(f)) if f != 0 else None for n_, v, f in
                                            zip(list(PARAM_NAMES) + ["rho_row%d" % i for i in range(B.rhos.size)],
@@ -982,8 +1187,65 @@ def run_gradient(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def run_profile_case(args):
+    """One propagation of an n x n grid (cosines in [-1, 0], energies log-spaced
+    over 0.1-1000 GeV, 11-shell body, nominal parameters), repeated, for a
+    profiler: the nine planes, fused event rates into 400 x 200 bins (flux
+    E^-2.7, nu_e = nu_mu / 2), planes averaged over 8 production heights
+    (10-45 km), or evaluations of the 400 x 200 binned log-likelihood and its
+    gradient (n does not apply).  Prints the wall time per calculation."""
+    import cudaprob3_gb300 as cp
+    from cudaprob3_gb300 import grids as G
+    if args.profile_case == "gradient":
+        from cudaprob3_gb300.loglik import binned_problem
+        prob = binned_problem(device_id=0)
+        L = prob.make(device_id=0, precision=args.precision)
+        L.evaluate(prob.nominal, prob.body.rhos)
+        t0 = time.perf_counter()
+        for _ in range(args.repeat):
+            L.evaluate(prob.nominal, prob.body.rhos)
+        dt = time.perf_counter() - t0
+        L.close()
+        print("gradient precision=%s repeat=%d: %.3f ms per evaluation" % (args.precision, args.repeat,
+                                                                           1e3 * dt / args.repeat))
+        return
+    n = args.n
+    c = G.linspace(-1.0, 0.0, n)
+    e = G.logspace(0.1, 1000.0, n)
+    B = G.PREM_12
+    with cp.CudaPropagatorSingle(0, n, n, precision=args.precision) as p:
+        p.setEnergyList(e)
+        p.setCosineList(c)
+        p.setMNSMatrix(*G.NOMINAL[:4])
+        p.setNeutrinoMasses(*G.NOMINAL[4:])
+        p.setDensity(B.radii, B.rhos, B.ye)
+        p.setProductionHeight(G.PRODUCTION_HEIGHT_KM)
+        if args.profile_case == "heights":
+            p.setProductionHeights(np.arange(10.0, 46.0, 5.0), [0.04, 0.10, 0.18, 0.22, 0.20, 0.14, 0.08, 0.04])
+        if args.profile_case == "rates":
+            phi = (e ** -2.7).astype(np.float32)
+            flux = np.zeros((3, n, n), np.float32)
+            flux[0] = 0.5 * phi[None, :]
+            flux[1] = phi[None, :]
+            p.setRateFlux(flux, 3)
+            p.setRateBins((np.arange(n) * 400) // n, (np.arange(n) * 200) // n, 400, 200)
+        t = cp.Antineutrino if args.anti else cp.Neutrino
+        t0 = time.perf_counter()
+        for _ in range(args.repeat):
+            if args.profile_case == "rates":
+                p.calculateRates(t)
+            else:
+                p.calculateProbabilities(t)
+        dt = time.perf_counter() - t0
+        print("n=%d precision=%s case=%s repeat=%d: %.3f ms per calculation" % (
+            n, args.precision, args.profile_case, args.repeat, 1e3 * dt / args.repeat))
+
+
 def main():
     args = parse()
+    if args.profile_case:
+        run_profile_case(args)
+        return
     world, rank, local = dist_init(args)
     try:
         if args.impl == "reference":

@@ -66,7 +66,6 @@ SIGNATURES = [
     ("cp3_autotune", _I, [_P, _I, _I, _IP, _IP, _IP, ctypes.POINTER(ctypes.c_float)]),
     ("cp3_set_kernel_timing", _I, [_P, _I]),
     ("cp3_last_kernel_ms", _I, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
-    ("cp3_pipe_peak", _I, [_I, _I, _DP]),
     ("cp3_batch_create", _I, [ctypes.POINTER(_P), _I, _I, _I, _IP, _IP]),
     ("cp3_batch_destroy", _I, [_P]),
     ("cp3_batch_set_grids", _I, [_P, _DP, _DP]),
@@ -94,13 +93,12 @@ SIGNATURES = [
     ("cp3_loglik_set_flux", _I, [_P, _DP, _DP, _D]),
     ("cp3_loglik_set_observed", _I, [_P, _DP]),
     ("cp3_loglik_evaluate", _I, [_P, _I, _DP, _DP, _DP, _DP]),
+    ("cp3_loglik_set_kernel_timing", _I, [_P, _I]),
+    ("cp3_loglik_last_kernel_ms", _I, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                       ctypes.POINTER(ctypes.c_float)]),
     ("cp3_propagate_noalloc", _I, [_I, _I, _P, _I, _P, _I, _DP, _DP, _DP, _I, _D, _D, _D, _D, _D, _D, _D, _P,
                                    _P]),
 ]
-
-PIPE_IMAD_WIDE = 0
-PIPE_FFMA = 1
-PIPE_DFMA = 2
 
 _lib = None
 

@@ -4,6 +4,8 @@
 
 The library is compiled with nvcc directly (no torch extension machinery):
 one -gencode for sm_103a, one process per translation unit, then a link step.
+The same call builds the benchmark's pipe probes (bench_pipes.cu beside
+bench.py) into libbench_pipes.so, a library of their own.
 """
 import os
 import subprocess
@@ -15,7 +17,11 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcudaprob3_gb300.so")
-SOURCES = ["cp3_abi.cu", "cp3_kernels.cu", "cp3_pipes.cu", "cp3_batch.cu", "cp3_loglik.cu", "cp3_noalloc.cu"]
+SOURCES = ["cp3_abi.cu", "cp3_kernels.cu", "cp3_batch.cu", "cp3_loglik.cu", "cp3_noalloc.cu"]
+# the benchmark's pipe-throughput probes: a library of their own, not part of
+# the propagator's library or public header
+BENCH_PIPES_SRC = os.path.join(ROOT, "bench_pipes.cu")
+BENCH_PIPES_LIB = os.path.join(ROOT, "libbench_pipes.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-fopenmp", "--expt-relaxed-constexpr",
               "-I" + os.path.join(ROOT, "include")]
@@ -69,6 +75,9 @@ def build(verbose=False, force=False):
         if r.returncode != 0:
             raise RuntimeError("nvcc failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
         return r.stderr
+    if force or not _newer(BENCH_PIPES_LIB, [BENCH_PIPES_SRC]) or not _loads_here(BENCH_PIPES_LIB):
+        jobs.append([nvcc()] + ARCH + ["-O3", "-std=c++17", "-shared", "-Xcompiler", "-fPIC", BENCH_PIPES_SRC,
+                                       "-o", BENCH_PIPES_LIB])
     with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         list(ex.map(run, jobs))
     if force or jobs or not _newer(LIB, objs) or not _loads_here(LIB):

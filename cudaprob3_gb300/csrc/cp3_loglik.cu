@@ -936,6 +936,11 @@ struct cp3_loglik {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int graph_type = -1;
+    // optional kernel timing: events recorded by the graph before the prep
+    // kernel and after each of the three kernels
+    bool timing = false;
+    bool timed = false;  // the last evaluation ran a graph with the events
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 namespace {
@@ -1075,6 +1080,11 @@ int ll_setup(cp3_loglik* L, int type) {
     e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     const cp3::LLArgs a = ll_args(L, type);
     if (!e) e = cudaMemcpyAsync(L->d_osc, L->h_up, kOscBlock + sizeof(double) * L->nl, cudaMemcpyHostToDevice, cs);
+    // event-record nodes around the kernels when timing is on
+    auto stamp = [&](int k) {
+        if (!e && L->timing) e = cudaEventRecordWithFlags(L->ev[k], cs, cudaEventRecordExternal);
+    };
+    stamp(0);
     if (!e) {
         // energies per prep block: enough blocks to spread the FP64
         // eigen-solves over the GPU (about two per SM), at most 256 threads
@@ -1086,6 +1096,7 @@ int ll_setup(cp3_loglik* L, int type) {
         cp3::ll_prep_kernel<<<nbE + nbC, dim3(L->nl, eb), (size_t)eb * L->nl * 9 * 8, cs>>>(a);
         e = cudaGetLastError();
     }
+    stamp(1);
     if (!e) {
         dim3 grid((L->n_en + 3) / 4, L->n_cchunk);
         if (L->mixed)
@@ -1094,6 +1105,7 @@ int ll_setup(cp3_loglik* L, int type) {
             cp3::ll_pair_kernel<double><<<grid, 128, 0, cs>>>(a);
         e = cudaGetLastError();
     }
+    stamp(2);
     if (!e) {
         // energies per block: the fewest warps on the busiest SM (the
         // kernel is bound by the FP64 issue of that SM), at most 288 threads
@@ -1112,6 +1124,7 @@ int ll_setup(cp3_loglik* L, int type) {
         cp3::ll_layer_kernel<<<(L->n_en + epb - 1) / epb, threads, smem, cs>>>(a, epb);
         e = cudaGetLastError();
     }
+    stamp(3);
     cudaGraph_t g = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(cs, &g);
     cudaStreamDestroy(cs);
@@ -1123,6 +1136,7 @@ int ll_setup(cp3_loglik* L, int type) {
     if ((e = cudaGraphInstantiate(&L->exec, g, 0))) return lcuda(e, "cudaGraphInstantiate");
     L->graph_type = type;
     L->dirty = false;
+    L->timed = L->timing;
     return CP3_OK;
 }
 
@@ -1164,6 +1178,8 @@ int cp3_loglik_destroy(cp3_loglik* L) {
     LGuard g(L->device);
     if (L->stream) cudaStreamSynchronize(L->stream);
     ll_free(L);
+    for (cudaEvent_t ev : L->ev)
+        if (ev) cudaEventDestroy(ev);
     if (L->h_up) cudaFreeHost(L->h_up);
     if (L->h_rows) cudaFreeHost(L->h_rows);
     if (L->stream) cudaStreamDestroy(L->stream);
@@ -1303,6 +1319,34 @@ int cp3_loglik_evaluate(cp3_loglik* L, int type, const double* params, const dou
     if (loglik) *loglik = s[0];
     if (grad)
         for (int q = 0; q < 6 + L->n_rows; q++) grad[q] = s[1 + q];
+    return CP3_OK;
+}
+
+int cp3_loglik_set_kernel_timing(cp3_loglik* L, int enable) {
+    if (!L) return lfail(CP3_ERR_ARGUMENT, "null argument");
+    LGuard g(L->device);
+    if (g.err) return lcuda(g.err, "cudaSetDevice");
+    if (enable && !L->ev[0])
+        for (cudaEvent_t& ev : L->ev) {
+            cudaError_t e = cudaEventCreate(&ev);
+            if (e) return lcuda(e, "cudaEventCreate");
+        }
+    if ((enable != 0) != L->timing) L->dirty = true;  // the graph is captured again with or without the events
+    L->timing = enable != 0;
+    return CP3_OK;
+}
+
+int cp3_loglik_last_kernel_ms(cp3_loglik* L, float* prep_ms, float* pair_ms, float* layer_ms) {
+    if (!L) return lfail(CP3_ERR_ARGUMENT, "null argument");
+    if (!L->timed || !L->exec) return lfail(CP3_ERR_STATE, "loglik_last_kernel_ms: no timed evaluation");
+    LGuard g(L->device);
+    float t[3] = {0, 0, 0};
+    cudaError_t e = cudaEventSynchronize(L->ev[3]);
+    for (int k = 0; k < 3 && !e; k++) e = cudaEventElapsedTime(&t[k], L->ev[k], L->ev[k + 1]);
+    if (e) return lcuda(e, "cudaEventElapsedTime");
+    if (prep_ms) *prep_ms = t[0];
+    if (pair_ms) *pair_ms = t[1];
+    if (layer_ms) *layer_ms = t[2];
     return CP3_OK;
 }
 

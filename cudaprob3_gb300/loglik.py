@@ -84,6 +84,17 @@ class LogLikelihood:
         check(self._lib.cp3_loglik_evaluate(self._h, int(ntype), _dp(p), _dp(r), ctypes.byref(ll), _dp(grad)))
         return ll.value, grad
 
+    def set_kernel_timing(self, enable):
+        """CUDA events around the evaluation's kernels (the graph is captured
+        again with or without them)."""
+        check(self._lib.cp3_loglik_set_kernel_timing(self._h, 1 if enable else 0))
+
+    def last_kernel_ms(self):
+        """(prep, pair, layer) kernel durations of the last timed evaluation."""
+        t = [ctypes.c_float() for _ in range(3)]
+        check(self._lib.cp3_loglik_last_kernel_ms(self._h, *[ctypes.byref(x) for x in t]))
+        return tuple(x.value for x in t)
+
 
 class BinnedProblem:
     """The inputs of a binned fit (see the module docstring)."""

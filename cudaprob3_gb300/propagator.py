@@ -50,13 +50,6 @@ def device_count():
     return int(_lib.load().cp3_device_count())
 
 
-def pipe_peak(pipe, device_id=0):
-    """Measured operations per second of one pipe (_lib.PIPE_*) on a device."""
-    out = ctypes.c_double()
-    check(_lib.load().cp3_pipe_peak(int(device_id), int(pipe), ctypes.byref(out)))
-    return out.value
-
-
 class CudaPropagatorSingle:
     """Single-GPU propagator: CudaPropagatorSingle(id, n_cosines, n_energies)."""
 
