@@ -112,7 +112,10 @@ struct Q30 {
     // Q2.60 probability -> float, one rounding; the completed entries of the
     // doubly stochastic matrix may come out a few 1e-10 below zero: clamp
     static __device__ __forceinline__ float to_prob(long long q) {
-        return q <= 0 ? 0.0f : __ll2float_rn(q) * 8.673617379884035e-19f;  // 2^-60
+        return q <= 0 ? 0.0f : q2_60_to_float(q);
+    }
+    static __device__ __forceinline__ float q2_60_to_float(long long q) {
+        return __ll2float_rn(q) * 8.673617379884035e-19f;  // 2^-60
     }
     // the nine probabilities from the 2x2 block B = (S[e][e], S[e][mu], S[mu][e], S[mu][mu])
     // of a unitary S: out[in*3+out] = |S[out][in]|^2, rows and columns summing to one
@@ -123,8 +126,9 @@ struct Q30 {
         const long long q02 = one - q00 - q01, q12 = one - q10 - q11;
         const long long q20 = one - q00 - q10, q21 = one - q01 - q11;
         const long long q22 = q00 + q01 + q10 + q11 - one;
-        out[0] = to_prob(q00); out[1] = to_prob(q10); out[2] = to_prob(q20);
-        out[3] = to_prob(q01); out[4] = to_prob(q11); out[5] = to_prob(q21);
+        // the four squared moduli are >= 0 and need no clamp (same bits)
+        out[0] = q2_60_to_float(q00); out[1] = q2_60_to_float(q10); out[2] = to_prob(q20);
+        out[3] = q2_60_to_float(q01); out[4] = q2_60_to_float(q11); out[5] = to_prob(q21);
         out[6] = to_prob(q02); out[7] = to_prob(q12); out[8] = to_prob(q22);
     }
     // averages over production heights: |z|^2 as a float (one rounding of the
