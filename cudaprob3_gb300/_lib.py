@@ -7,7 +7,10 @@ import ctypes
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libcudaprob3_gb300.so")
+# CUDAPROB3_GB300_LIBRARY selects another build of the same library, e.g. the
+# bounds-checked libcudaprob3_gb300_check.so
+LIB_PATH = os.environ.get("CUDAPROB3_GB300_LIBRARY") or os.path.join(HERE, "libcudaprob3_gb300.so")
+CHECK_LIB_PATH = os.path.join(HERE, "libcudaprob3_gb300_check.so")
 
 # status codes (include/cudaprob3_gb300.h)
 OK = 0
@@ -17,6 +20,7 @@ ERR_CUDA = -3
 ERR_NO_DEVICE = -4
 ERR_FILE = -5
 ERR_LIMIT = -6
+ERR_CHECK = -7
 
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
@@ -30,6 +34,7 @@ _IP = ctypes.POINTER(ctypes.c_int)
 _SZ = ctypes.c_size_t
 SIGNATURES = [
     ("cp3_abi_version", _I, []),
+    ("cp3_bounds_checked", _I, []),
     ("cp3_last_error", ctypes.c_char_p, []),
     ("cp3_device_count", _I, []),
     ("cp3_create", _I, [ctypes.POINTER(_P), _I, _I, _I, _I]),
@@ -117,7 +122,7 @@ def load():
     global _lib
     if _lib is None:
         if not os.path.exists(LIB_PATH):
-            raise ImportError("libcudaprob3_gb300.so is not built: run `python -m cudaprob3_gb300.build`")
+            raise ImportError("%s is not built: run `python -m cudaprob3_gb300.build`" % os.path.basename(LIB_PATH))
         lib = ctypes.CDLL(LIB_PATH)
         for name, res, args in SIGNATURES:
             fn = getattr(lib, name)

@@ -4,8 +4,12 @@
 
 The library is compiled with nvcc directly (no torch extension machinery):
 one -gencode for sm_103a, one process per translation unit, then a link step.
-The same call builds the benchmark's pipe probes (bench_pipes.cu beside
-bench.py) into libbench_pipes.so, a library of their own.
+The same call builds the bounds-checked debug library
+libcudaprob3_gb300_check.so (the same sources with -DCP3_CHECK: every kernel
+index compared with its buffer's extent, failures reported as CP3_ERR_CHECK;
+select it with CUDAPROB3_GB300_LIBRARY=<path>) and the benchmark's pipe
+probes (bench_pipes.cu beside bench.py) into libbench_pipes.so, a library of
+their own.
 """
 import os
 import subprocess
@@ -17,6 +21,9 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcudaprob3_gb300.so")
+# the bounds-checked debug build of the same sources (-DCP3_CHECK)
+BUILD_CHECK = os.path.join(HERE, "_build_check")
+LIB_CHECK = os.path.join(HERE, "libcudaprob3_gb300_check.so")
 SOURCES = ["cp3_abi.cu", "cp3_kernels.cu", "cp3_batch.cu", "cp3_loglik.cu", "cp3_noalloc.cu"]
 # the benchmark's pipe-throughput probes: a library of their own, not part of
 # the propagator's library or public header
@@ -56,18 +63,30 @@ def _loads_here(path):
         return False
 
 
-def build(verbose=False, force=False):
-    """Compile every translation unit for sm_103a and link the shared library."""
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose=False, force=False, check=True):
+    """Compile every translation unit for sm_103a and link the shared library
+    (and, with check, the bounds-checked library), all nvcc processes in
+    parallel."""
     heads = _headers()
-    objs = []
     jobs = []
-    for src in SOURCES:
-        s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
-        objs.append(o)
-        if force or not _newer(o, [s] + heads):
-            jobs.append([nvcc()] + ARCH + NVCC_FLAGS + ["-c", s, "-o", o])
+    links = []
+    for build_dir, lib, extra in ((BUILD, LIB, []), (BUILD_CHECK, LIB_CHECK, ["-DCP3_CHECK"]))[:2 if check else 1]:
+        os.makedirs(build_dir, exist_ok=True)
+        objs = []
+        fresh = True
+        for src in SOURCES:
+            s = os.path.join(CSRC, src)
+            o = os.path.join(build_dir, src.replace(".cu", ".o"))
+            objs.append(o)
+            if force or not _newer(o, [s] + heads):
+                jobs.append([nvcc()] + ARCH + NVCC_FLAGS + extra + ["-c", s, "-o", o])
+                fresh = False
+        if force or not fresh or not _newer(lib, objs) or not _loads_here(lib):
+            links.append([nvcc()] + ARCH + ["-shared", "-Xcompiler", "-fopenmp", "-o", lib] + objs)
+    if force or not _newer(BENCH_PIPES_LIB, [BENCH_PIPES_SRC]) or not _loads_here(BENCH_PIPES_LIB):
+        jobs.append([nvcc()] + ARCH + ["-O3", "-std=c++17", "-shared", "-Xcompiler", "-fPIC", BENCH_PIPES_SRC,
+                                       "-o", BENCH_PIPES_LIB])
+
     def run(cmd):
         if verbose:
             print(" ".join(cmd), flush=True)
@@ -75,13 +94,9 @@ def build(verbose=False, force=False):
         if r.returncode != 0:
             raise RuntimeError("nvcc failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
         return r.stderr
-    if force or not _newer(BENCH_PIPES_LIB, [BENCH_PIPES_SRC]) or not _loads_here(BENCH_PIPES_LIB):
-        jobs.append([nvcc()] + ARCH + ["-O3", "-std=c++17", "-shared", "-Xcompiler", "-fPIC", BENCH_PIPES_SRC,
-                                       "-o", BENCH_PIPES_LIB])
-    with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+    with ThreadPoolExecutor(max_workers=max(1, len(jobs), len(links))) as ex:
         list(ex.map(run, jobs))
-    if force or jobs or not _newer(LIB, objs) or not _loads_here(LIB):
-        run([nvcc()] + ARCH + ["-shared", "-Xcompiler", "-fopenmp", "-o", LIB] + objs)
+        list(ex.map(run, links))
     return LIB
 
 

@@ -65,6 +65,13 @@ struct DevBuf {
 
 namespace cp3 {
 void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+int check_status(const CheckRecord& r) {
+    if (r.count == 0) return CP3_OK;
+    return fail(CP3_ERR_CHECK, std::string("bounds check failed: ") + check_site_name(r.site) + ", index " +
+                                   std::to_string(r.index) + " not in [0, " + std::to_string(r.bound) + ") (" +
+                                   std::to_string(r.count) + " failed checks)");
+}
 }  // namespace cp3
 
 struct cp3_propagator {
@@ -184,6 +191,8 @@ void complete_planes_on_host(T* h, size_t plane) {
 extern "C" {
 
 int cp3_abi_version(void) { return CP3_ABI_VERSION; }
+
+int cp3_bounds_checked(void) { return cp3::kChecked ? 1 : 0; }
 
 const char* cp3_last_error(void) { return g_last_error.c_str(); }
 
@@ -732,6 +741,11 @@ int cp3_wait_for_completion(cp3_propagator* p) {
     DeviceGuard g(p->device);
     cudaError_t e = cudaStreamSynchronize(p->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+    if (cp3::kChecked) {  // the bounds-checked build reports the calculation's failed checks here
+        cp3::CheckRecord r{};
+        if ((e = cp3::kernels_check_take(&r)) != cudaSuccess) return cuda_fail(e, "bounds-check record");
+        if (int rc = cp3::check_status(r)) return rc;
+    }
     if (p->completion_pending) {
         const size_t plane = (size_t)p->n_cos * p->n_en;
         if (p->mixed)

@@ -18,6 +18,9 @@
 
 #include <cstdint>
 
+#include "cp3_check.cuh"
+#include "cp3_internal.h"
+
 namespace cp3 {
 
 // ---------------------------------------------------------------- Q1.30 ----
@@ -170,7 +173,7 @@ __device__ __forceinline__ void turns_q30_u(float u, float e, const int4* __rest
     const float d2 = d * d;
     const float sx = d * fmaf(d2, -4.134170224e+01f, 6.283185307e+00f);
     const float cm = d2 * fmaf(d2, 6.493939402e+01f, -1.973920880e+01f);
-    const int4 t = tab[(int)j + 128];
+    const int4 t = tab[CP3_IX(kSitePhaseTable, (int)j + 128, kPhaseTabN + 1)];
     const float cf = __int_as_float(t.z), sf = __int_as_float(t.w);
     const float dc = fmaf(cf, cm, -sf * sx);  // Q1.30 units
     const float ds = fmaf(sf, cm, cf * sx);

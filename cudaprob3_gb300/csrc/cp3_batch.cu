@@ -57,7 +57,18 @@ struct BatchPrepArgs {
     void* tab;
     void* pe;
     void* len;
+    // extents for the checked build: sets, table words, length entries
+    int n_sets;
+    long long tab_words, pe_words, len_entries;
 };
+
+// Checked build: the tables of set `gr` lie inside the batch's buffers.
+__device__ __forceinline__ bool batch_grid_ok(const BatchGrid& gr, int nl, int nl_pad, int W, long long tab_words,
+                                              long long pe_words, long long len_entries) {
+    return check_ok(kSiteBatchTile, gr.tab_off + (long long)gr.n_en_pad * nl * W - 1, tab_words) &&
+           check_ok(kSiteBatchTile, gr.pe_off + (long long)kPerEWords * gr.n_en_pad - 1, pe_words) &&
+           (gr.n_cos == 0 || check_ok(kSiteBatchTile, gr.len_off + (long long)gr.n_cos * nl_pad - 1, len_entries));
+}
 
 template <bool MIXED>
 __device__ __forceinline__ void batch_prep_item(const BatchPrepArgs& a, int bid) {
@@ -65,9 +76,14 @@ __device__ __forceinline__ void batch_prep_item(const BatchPrepArgs& a, int bid)
     const int nl = a.nl;
     // cosine blocks first: blocks dispatch in index order, and the short
     // cosine blocks would otherwise trail the eigen-solves
+    const int W = MIXED ? kMixedWords : kFp64Words;
     if ((int)bid >= a.n_cblk) {
         const int2 b = a.eblk[bid - a.n_cblk];
+        if (!check_ok(kSiteBatchSet, b.x, a.n_sets)) return;  // b is the same for the whole block
         const BatchGrid& gr = a.grids[b.x];
+        if (!(batch_grid_ok(gr, nl, a.nl_pad, W, a.tab_words, a.pe_words, a.len_entries) &&
+              check_ok(kSiteBatchPrep, b.y, gr.n_en_pad)))
+            return;
         const size_t word = MIXED ? 4 : 8;
         const GridTables g{(unsigned char*)a.tab + gr.tab_off * word, (unsigned char*)a.pe + gr.pe_off * word,
                            (unsigned char*)a.len + gr.len_off * 8, gr.n_en_pad, a.te, nl, a.nl_pad};
@@ -99,7 +115,9 @@ __device__ __forceinline__ void batch_prep_item(const BatchPrepArgs& a, int bid)
         }
     } else {
         const int2 b = a.cblk[bid];
+        if (!check_ok(kSiteBatchSet, b.x, a.n_sets)) return;
         const BatchGrid& gr = a.grids[b.x];
+        if (!batch_grid_ok(gr, nl, a.nl_pad, W, a.tab_words, a.pe_words, a.len_entries)) return;
         // one thread per (cosine, layer): b.y is the block's first flat index
         const int f = b.y + threadIdx.y * blockDim.x + threadIdx.x;
         const int c = f / a.nl_pad, l = f % a.nl_pad;
@@ -132,6 +150,9 @@ struct BatchPropArgs {
     const int4* ptab;
     void* out;
     int nl, nl_pad, cchunk;
+    // extents for the checked build
+    int n_sets;
+    long long tab_words, pe_words, len_entries, out_elems;
 };
 
 template <bool MIXED, int TE>
@@ -148,7 +169,10 @@ __global__ void __launch_bounds__(MIXED ? 256 : 128, MIXED ? 4 : 3) batch_propag
         const int it = s_item;
         if (it >= a.n_items) break;
         const int4 w = a.items[it];
-        const BatchGrid& g = a.grids[w.x];
+        // checked build: the item names a set whose tables and planes lie in
+        // the batch's buffers (w is the same for the whole block)
+        const bool item_ok = check_ok(kSiteBatchSet, w.x, a.n_sets);
+        const BatchGrid& g = a.grids[item_ok ? w.x : 0];
         TileJob j;
         j.tab = (const unsigned char*)a.tab + g.tab_off * word;
         j.pe = (const unsigned char*)a.pe + g.pe_off * word;
@@ -161,7 +185,11 @@ __global__ void __launch_bounds__(MIXED ? 256 : 128, MIXED ? 4 : 3) batch_propag
         j.etile = w.y;
         j.c0 = w.z;
         j.ncl = w.w;
-        process_tile<MIXED, TE>(j, a.nl, a.nl_pad, smem, L);
+        if (item_ok && batch_grid_ok(g, a.nl, a.nl_pad, MIXED ? kMixedWords : kFp64Words, a.tab_words, a.pe_words,
+                                     a.len_entries) &&
+            ((long long)g.n_cos * g.n_en == 0 ||
+             check_ok(kSiteBatchTile, g.out_off + 9LL * g.n_cos * g.n_en - 1, a.out_elems)))
+            process_tile<MIXED, TE>(j, a.nl, a.nl_pad, smem, L);
         __syncthreads();
     }
 }
@@ -535,6 +563,10 @@ cp3::BatchPrepArgs prep_args(cp3_batch* b, int k) {
     a.tab = b->d_tab.p;
     a.pe = b->d_pe.p;
     a.len = b->d_len.p;
+    a.n_sets = b->n_sets;
+    a.tab_words = (long long)(b->d_tab.n / (b->mixed ? 4 : 8));
+    a.pe_words = (long long)(b->d_pe.n / (b->mixed ? 4 : 8));
+    a.len_entries = (long long)(b->d_len.n / 8);
     return a;
 }
 
@@ -553,6 +585,11 @@ cp3::BatchPropArgs prop_args(cp3_batch* b, int k) {
     a.nl = b->nl;
     a.nl_pad = b->nl_pad;
     a.cchunk = b->cchunk;
+    a.n_sets = b->n_sets;
+    a.tab_words = (long long)(b->d_tab.n / (b->mixed ? 4 : 8));
+    a.pe_words = (long long)(b->d_pe.n / (b->mixed ? 4 : 8));
+    a.len_entries = (long long)(b->d_len.n / 8);
+    a.out_elems = (long long)(b->d_out.n / b->elem());
     return a;
 }
 
@@ -864,6 +901,13 @@ int cp3_batch_wait(cp3_batch* b) {
     if (e) return bcuda(e, "cudaStreamSynchronize");
     float ms = 0;
     if (cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]) == cudaSuccess) b->last_ms = ms;
+    // checked build: this file's kernels and the single-grid kernels of the
+    // sequential path (nothing to read otherwise)
+    if (cp3::kChecked) {
+        cp3::CheckRecord r{}, r2{};
+        if ((e = cp3::check_take(&r)) || (e = cp3::kernels_check_take(&r2))) return bcuda(e, "bounds-check record");
+        if (int rc = cp3::check_status(r.count ? r : r2)) return rc;
+    }
     return CP3_OK;
 }
 

@@ -60,6 +60,7 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a) {
         if (c >= a.pb.n_cos) return;
         const double cz = a.pb.cosines[c];
         const int M = a.pb.maxlayers[c];
+        if (!check_ok(kSitePrepLayer, M, nl)) return;
         prep_cosine_layer<MIXED>(cz, M, a.pb.radii, a.pb.height_cm, c, l, g);
         // atmosphere segment at every production height (physics.hpp:613-616,
         // 561-562), spread over the cosine's layer threads
@@ -112,6 +113,8 @@ __global__ void __launch_bounds__(MIXED ? 256 : 128, (MIXED && MODE != kModeHeig
 }
 
 // ------------------------------------------------------------- launchers ----
+cudaError_t kernels_check_take(CheckRecord* out) { return check_take(out); }
+
 int max_dynamic_smem() {
     int dev = 0, v = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||

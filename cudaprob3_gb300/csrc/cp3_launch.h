@@ -8,6 +8,7 @@
 #include <cstring>
 #include <string>
 
+#include "cp3_check.cuh"
 #include "cp3_internal.h"
 
 namespace cp3 {
@@ -126,5 +127,13 @@ inline const char* order_body(const double* radii, const double* rhos, const dou
 
 // Message returned by cp3_last_error() on this thread.
 void set_last_error(const std::string& msg);
+
+// Checked build: reads and clears the check record of the single-grid
+// kernels (prep_kernel, propagate_kernel); an empty record otherwise.
+cudaError_t kernels_check_take(CheckRecord* out);
+
+// CP3_OK for an empty record; otherwise CP3_ERR_CHECK with the first failed
+// check (site, index, extent) and the count as the last error.
+int check_status(const CheckRecord& r);
 
 }  // namespace cp3

@@ -291,8 +291,9 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) ll_pair_kernel(LL
     const int cchunk = blockIdx.y;
     const int c = cchunk * 32 + lane;
     if (e >= a.n_en) return;  // whole warp leaves together
+    if (!check_ok(kSiteLLPair, cchunk, a.n_cchunk)) return;  // the same for the whole block
     const bool valid = c < a.n_cos;
-    const int M = valid ? a.maxl[c] : 0;
+    const int M = valid ? CP3_IX(kSiteLLPair, a.maxl[c], a.nl) : 0;
     const int Mw = __reduce_max_sync(0xffffffffu, M);
     const LLSrc<R> src(a, e, valid ? c : 0);
     const R twopi = (R)kTwoPi;
@@ -856,7 +857,8 @@ __global__ void __launch_bounds__(288) ll_layer_kernel(LLArgs a, int epb) {
         if (l >= 1 && r == 0) {
             const double sgn = a.anti ? 1.0 : -1.0;
             const int np = 6 + a.n_rows;
-            a.part_g[(size_t)e * (1 + np) + 1 + 6 + a.layer_row[l]] = -hr[0] * sgn * kGF * E * a.ye_layer[l];
+            a.part_g[(size_t)e * (1 + np) + 1 + 6 + CP3_IX(kSiteLLLayer, a.layer_row[l], a.n_rows)] =
+                -hr[0] * sgn * kGF * E * a.ye_layer[l];
         }
 #pragma unroll
         for (int q = 0; q < kLLOscOut; q++) sAcc[w * kLLOscOut + q] = acc[q];
@@ -1308,6 +1310,11 @@ int cp3_loglik_evaluate(cp3_loglik* L, int type, const double* params, const dou
     cudaError_t e = cudaGraphLaunch(L->exec, L->stream);
     if (!e) e = cudaStreamSynchronize(L->stream);
     if (e) return lcuda(e, "loglik evaluation");
+    if (cp3::kChecked) {  // the bounds-checked build reports failed checks of this evaluation
+        cp3::CheckRecord r{};
+        if ((e = cp3::check_take(&r))) return lcuda(e, "bounds-check record");
+        if (int rc = cp3::check_status(r)) return rc;
+    }
     // fixed-order sums of the energies' rows (slot 0 the log-likelihood, then
     // the 6 oscillation parameters and the density rows)
     const int np1 = 7 + L->n_rows;

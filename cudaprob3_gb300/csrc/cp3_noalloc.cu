@@ -71,13 +71,13 @@ struct NoAllocBody {
 __global__ void noalloc_setup_kernel(NoAllocBody body, const double* cosines, int n_cos, double* radii,
                                      double* rhoye, int* maxl) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < body.n) radii[t] = body.radii[t];
-    if (t <= body.n) rhoye[t] = body.rhoye[t];
+    if (t < body.n) radii[CP3_IX(kSiteNoAlloc, t, kNoAllocMaxLayers)] = body.radii[t];
+    if (t <= body.n) rhoye[CP3_IX(kSiteNoAlloc, t, kNoAllocMaxLayers)] = body.rhoye[t];
     if (t < n_cos) {
         const double cz = cosines[t];
         int cnt = 0;
         for (int i = 0; i < body.n; i++) cnt += (cz < body.coslimit[i]);
-        maxl[t] = cnt;
+        maxl[CP3_IX(kSiteNoAlloc, t, kNoAllocMaxCosines)] = cnt;
     }
 }
 
@@ -221,5 +221,14 @@ extern "C" int cp3_propagate_noalloc(int precision, int type, const double* d_co
     const size_t smem = propagate_smem_bytes(mixed, te, nl, nl_pad, cchunk);
     if ((e = launch_propagate(mixed, ka, te, groups, smem, s)) != cudaSuccess)
         return nfail(CP3_ERR_CUDA, std::string("propagate kernel: ") + cudaGetErrorString(e));
+    if (kChecked) {
+        // the bounds-checked build waits for the call and reports its failed
+        // checks (the set-up kernel's, and the prep and propagate kernels')
+        CheckRecord r{}, r2{};
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess || (e = check_take(&r)) != cudaSuccess ||
+            (e = kernels_check_take(&r2)) != cudaSuccess)
+            return nfail(CP3_ERR_CUDA, std::string("bounds-check record: ") + cudaGetErrorString(e));
+        if (int rc = check_status(r.count ? r : r2)) return rc;
+    }
     return CP3_OK;
 }

@@ -15,6 +15,7 @@
 #include <type_traits>
 
 #include "cp3_chain.cuh"
+#include "cp3_check.cuh"
 #include "cp3_internal.h"
 #include "cp3_physics.cuh"
 
@@ -37,6 +38,7 @@ __device__ __forceinline__ void prep_energy_layer(const OscParams& osc, double E
                                                   const GridTables& g, double* vme, double* m_out = nullptr) {
     const int te = g.te, tile = e / te, lane = e % te;
     const int W = MIXED ? kMixedWords : kFp64Words;
+    if (!(check_ok(kSitePrepTab, tile, g.n_en_pad / te) && check_ok(kSitePrepLayer, l, g.nl))) return;
     double m[3], V[9];
     layer_eigen(osc, E, rhoye, m, V);
     for (int w = 0; w < 9; w++) vme[w] = V[w];
@@ -90,6 +92,7 @@ template <bool MIXED>
 __device__ __forceinline__ void prep_overlap_v(int l, int e, const GridTables& g, const double* v, const double* vn) {
     const int te = g.te, tile = e / te, lane = e % te;
     const int W = MIXED ? kMixedWords : kFp64Words;
+    if (!(check_ok(kSitePrepTab, tile, g.n_en_pad / te) && check_ok(kSitePrepLayer, l, g.nl))) return;
     const size_t base = ((size_t)tile * g.nl + l) * W * te + lane;
 #pragma unroll
     for (int i = 0; i < 3; i++)
@@ -117,6 +120,8 @@ __device__ __forceinline__ void prep_overlap(int l, int e, const GridTables& g, 
 template <bool MIXED>
 __device__ __forceinline__ void prep_cosine_layer(double cz, int M, const double* radii, double height_cm, int c,
                                                   int l, const GridTables& g) {
+    // the chord of layer l reads the density rows up to M
+    if (!(check_ok(kSitePrepLayer, M, g.nl) && check_ok(kSitePrepLen, l, g.nl_pad))) return;
     const double L = (l <= M) ? layer_length_km(radii, l, M, cz, path_length_cm(cz, height_cm)) : 0.0;
     const size_t idx = (size_t)c * g.nl_pad + l;
     if (MIXED) {
@@ -318,7 +323,7 @@ __device__ __forceinline__ void flush_rates(Acc& s0, Acc& s1, Acc& s2, int cb, i
             }
             if (lane != lo) eb = -1;
         }
-        if (eb >= 0) {
+        if (eb >= 0 && check_ok(kSiteTileHist, cb, j.n_cb) && check_ok(kSiteTileHist, eb, j.n_eb)) {
             const size_t pl = (size_t)j.n_cb * j.n_eb;
             double* h = j.hist + (size_t)cb * j.n_eb + eb;
             atomicAdd(h, (double)s0);
@@ -354,6 +359,14 @@ __device__ __forceinline__ void process_tile(const TileJob& j, int nl, int nl_pa
     constexpr bool RATES = MODE == kModeRates;
     using Word = typename std::conditional<MIXED, int, double>::type;
     constexpr int W = MIXED ? kMixedWords : kFp64Words;
+    // checked build: the tile must lie in the grid's tables and its cosine
+    // rows in the grid and in the staged chunk (the same for every thread of
+    // the block, so a bad tile is skipped by the whole block)
+    if (!(check_ok(kSiteTileTab, j.etile, j.n_en_pad / TE) &&
+          (j.ncl <= 0 || (check_ok(kSiteTileChunk, j.ncl - 1, (long long)((L.cbin - L.maxl) / 4)) &&
+                          check_ok(kSiteTileLen, j.c0, j.n_cos) &&
+                          check_ok(kSiteTileLen, (long long)j.c0 + j.ncl - 1, j.n_cos)))))
+        return;
     Word* s_tab = (Word*)(smem + L.tab);
     Word* s_pe = (Word*)(smem + L.pe);
     const int4* s_ptab = (const int4*)(smem + L.ptab);
@@ -389,7 +402,7 @@ __device__ __forceinline__ void process_tile(const TileJob& j, int nl, int nl_pa
     int run_cb = -1;
     const int my_eb = (RATES && store) ? j.ebin[e] : -1;
     for (int cl = threadIdx.y; cl < j.ncl; cl += blockDim.y) {
-        const int M = s_maxl[cl];
+        const int M = CP3_IX(kSiteTileLayers, s_maxl[cl], nl);
         const int ci = j.c0 + cl;
         if (MIXED) {
             MixedSrc<TE> src{(const int*)s_tab + lane, (const int*)s_pe + lane,

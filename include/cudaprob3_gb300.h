@@ -44,6 +44,7 @@ extern "C" {
 #define CP3_ERR_NO_DEVICE (-4) /* no GPU, or the device id does not exist     */
 #define CP3_ERR_FILE (-5)      /* density file could not be opened            */
 #define CP3_ERR_LIMIT (-6)     /* a size exceeds a documented limit           */
+#define CP3_ERR_CHECK (-7)     /* bounds-checked build: a kernel index failed  */
 
 /* arithmetic of a propagator */
 #define CP3_PRECISION_FP64 0  /* plain method: every step in FP64              */
@@ -59,6 +60,17 @@ typedef struct cp3_propagator cp3_propagator;
 
 /* Version of this ABI (CP3_ABI_VERSION). */
 int cp3_abi_version(void);
+
+/* 1 in the bounds-checked debug build (libcudaprob3_gb300_check.so, compiled
+ * with -DCP3_CHECK), 0 otherwise.  No reference counterpart: the reference
+ * indexes its device arrays unchecked (physics.hpp:689-696).  In the checked
+ * build every shared- and global-memory index of the kernels is compared with
+ * its buffer's extent; a failure is recorded (never a trap), the access is
+ * kept inside the buffer, and the wait that ends the calculation
+ * (cp3_wait_for_completion, cp3_batch_wait, cp3_loglik_evaluate, and the
+ * no-allocation call, which waits in this build) returns CP3_ERR_CHECK with
+ * the kernel, index and extent in cp3_last_error(). */
+int cp3_bounds_checked(void);
 
 /* Message of the last failure on this thread ("" when none). */
 const char* cp3_last_error(void);
