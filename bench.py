@@ -145,11 +145,13 @@ def ll_pair_products_per_pair(M):
 # describes the kernel, and the roofline's traffic is reported as null.
 TRAFFIC_BYTES_PER_PAIR = 547_799_552 / (4096 * 4096)
 TRAFFIC_SOURCES_SHA = "c19b726b7be8342e5f74ccaccda0114d3a6c83aeffddbbc79acdedb78aec6253"
-TRAFFIC_SOURCES = ("cp3_arith.cuh", "cp3_chain.cuh", "cp3_internal.h", "cp3_physics.cuh", "cp3_tile.cuh")
+TRAFFIC_SOURCES = ("cp3_arith.cuh", "cp3_chain.cuh", "cp3_check.cuh", "cp3_internal.h", "cp3_kernels.cu",
+                   "cp3_physics.cuh", "cp3_tile.cuh")
 
 
 def traffic_sources_sha():
-    """SHA-256 over the device sources of the propagate kernel's body."""
+    """SHA-256 over the sources the propagate kernel is compiled from (its
+    body, its launch bounds and the helpers it inlines)."""
     import hashlib
     h = hashlib.sha256()
     for name in TRAFFIC_SOURCES:

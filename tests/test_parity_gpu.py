@@ -342,6 +342,43 @@ def test_configs2_scale_parameter_sets(gpu):
     torch.cuda.empty_cache()
 
 
+@pytest.mark.parametrize("which", ["dm21_zero", "dm32_zero"])
+def test_degenerate_masses_at_scale(gpu, which):
+    """The degeneracy breaks of setNeutrinoMasses (propagator.hpp:233-236: an
+    eigenvalue gap of 5e-9 eV^2) on the 4096 x 4096 grid, both neutrino types:
+    mixed against FP64 on every pair (max |dP| <= 1e-6, mean <= 1e-7), FP64
+    against the oracle on every 64th cosine and energy (1e-9, the degenerate
+    cases' tolerance: the reference itself loses accuracy as eps*|H|/gap)."""
+    torch = pytest.importorskip("torch")
+    n = 4096
+    c = G.linspace(-1, 0, n)
+    e = G.logspace(0.1, 1000, n)
+    B = G.PREM_12
+    params = list(G.NOMINAL)
+    params[4 if which == "dm21_zero" else 5] = 0.0
+    params = tuple(params)
+    pf = make(gpu, "fp64", c, e, B.radii, B.rhos, B.ye, params)
+    pm = make(gpu, "mixed", c, e, B.radii, B.rhos, B.ye, params)
+    bf = torch.empty((9, n, n), dtype=torch.float64, device="cuda:0")
+    bm = torch.empty((9, n, n), dtype=torch.float32, device="cuda:0")
+    pf.set_result_buffer(bf.data_ptr(), bf.numel() * 8)
+    pm.set_result_buffer(bm.data_ptr(), bm.numel() * 4)
+    idx = np.arange(0, n, 64)
+    for anti in (False, True):
+        t = gpu.Antineutrino if anti else gpu.Neutrino
+        pf.calculateProbabilities(t)
+        pm.calculateProbabilities(t)
+        d = (bm.double() - bf).abs_()
+        assert float(d.max()) <= 1e-6 and float(d.mean()) <= 1e-7, (which, anti, float(d.max()))
+        del d
+        want = oracle.calculate(c[idx], e[idx], B.radii, B.rho_eff(), params, 22.0, anti)
+        assert np.abs(bf[:, idx][:, :, idx].cpu().numpy() - want).max() <= 1e-9
+    pf.close()
+    pm.close()
+    del bf, bm
+    torch.cuda.empty_cache()
+
+
 def test_pipe_peaks_are_plausible(gpu):
     """The roofline denominators of bench.py (bench_pipes.cu, a library of its
     own): each probe's rate per SM and per clock, at the SM clock the probe
