@@ -57,8 +57,11 @@ def parse():
                          "graph launch; precision: 64 parameter sets on the 8192 x 8192 grid")
     ap.add_argument("--sets", type=int, default=0, help="number of parameter sets (batch/precision)")
     # one small case for profilers (ncu): no timing contract, no JSON line
-    ap.add_argument("--profile-case", choices=["planes", "rates", "heights", "gradient"], default=None,
-                    help="run one square grid (or the gradient evaluation) for a profiler instead of a benchmark")
+    ap.add_argument("--profile-case", choices=["planes", "rates", "heights", "gradient", "bands"], default=None,
+                    help="run one square grid (or the gradient evaluation, or fixed-layer-count bands) for a "
+                         "profiler instead of a benchmark")
+    ap.add_argument("--bands", type=int, nargs="*", default=[2, 3, 4, 7, 11],
+                    help="profile case bands: crossed-shell counts M, one launch each")
     ap.add_argument("--n", type=int, default=2048, help="profile case: cosines = energies")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed", help="profile case: arithmetic")
     ap.add_argument("--repeat", type=int, default=1, help="profile case: calculations")
@@ -143,8 +146,8 @@ def ll_pair_products_per_pair(M):
 # 4096 x 4096 launch, and the SHA-256 of the device sources the kernel was
 # compiled from at that capture.  When the sources differ the figure no longer
 # describes the kernel, and the roofline's traffic is reported as null.
-TRAFFIC_BYTES_PER_PAIR = 547_799_552 / (4096 * 4096)
-TRAFFIC_SOURCES_SHA = "c19b726b7be8342e5f74ccaccda0114d3a6c83aeffddbbc79acdedb78aec6253"
+TRAFFIC_BYTES_PER_PAIR = 547_072_512 / (4096 * 4096)
+TRAFFIC_SOURCES_SHA = "2f2385ceb3766bdf95fdb1e8af0e23b16c0752a5d1720b79dab555777ed0f685"
 TRAFFIC_SOURCES = ("cp3_arith.cuh", "cp3_chain.cuh", "cp3_check.cuh", "cp3_internal.h", "cp3_kernels.cu",
                    "cp3_physics.cuh", "cp3_tile.cuh")
 
@@ -1198,6 +1201,30 @@ def run_profile_case(args):
     gradient (n does not apply).  Prints the wall time per calculation."""
     import cudaprob3_gb300 as cp
     from cudaprob3_gb300 import grids as G
+    if args.profile_case == "bands":
+        # one launch per crossed-shell count M: 256 cosines strictly inside the
+        # band of M shells (between the M-th and (M+1)-th cosine limits of
+        # the 11-shell body) x 1024 energies, so that per-pair counters of
+        # the launches separate the cost of an inner layer from the fixed part
+        B = G.PREM_12
+        r = np.sort(B.radii)[::-1]
+        lim = -np.sqrt(1.0 - (r / 6371.0) ** 2)
+        lim[0] = 0.0
+        en = G.logspace(0.1, 1000.0, 1024)
+        for M in args.bands:
+            c = np.linspace(lim[M], lim[M - 1], 258)[1:-1]
+            with cp.CudaPropagatorSingle(0, c.size, en.size, precision=args.precision) as p:
+                p.setEnergyList(en)
+                p.setCosineList(c)
+                p.setMNSMatrix(*G.NOMINAL[:4])
+                p.setNeutrinoMasses(*G.NOMINAL[4:])
+                p.setDensity(B.radii, B.rhos, B.ye)
+                p.setProductionHeight(G.PRODUCTION_HEIGHT_KM)
+                if not (p.maxlayers() == M).all():
+                    raise RuntimeError("band %d: cosines outside the band" % M)
+                p.calculateProbabilities(cp.Neutrino)
+            print("band M=%d: %d x %d pairs" % (M, c.size, en.size), flush=True)
+        return
     if args.profile_case == "gradient":
         from cudaprob3_gb300.loglik import binned_problem
         prob = binned_problem(device_id=0)
