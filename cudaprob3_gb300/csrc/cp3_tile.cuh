@@ -29,6 +29,20 @@ struct GridTables {
     int n_en_pad, te, nl, nl_pad;
 };
 
+// Layout of the mixed tables' words, so that a lane reads its words with 16-byte
+// loads.  An (energy-tile, layer) block of the mixed table holds 13 words per
+// energy of the tile (te energies): words 0-11 as three groups of four
+// consecutive words per energy ([3][te][4]), word 12 on its own ([te]).  The
+// per-energy table in shared memory (18 words) is four groups of four
+// ([4][te][4]) and a pair ([te][2]).  Both take exactly the space of the
+// word-major layout ([13][te], [18][te]).
+__host__ __device__ inline int mixed_word_offset(int w, int lane, int te) {
+    return w < 12 ? (w >> 2) * 4 * te + lane * 4 + (w & 3) : 12 * te + lane;
+}
+__host__ __device__ inline int mixed_pe_offset(int w, int lane, int te) {
+    return w < 16 ? (w >> 2) * 4 * te + lane * 4 + (w & 3) : 16 * te + lane * 2 + (w - 16);
+}
+
 // Thread (l, e) of the energy part: eigen-solve of layer l at energy E, writes
 // kappa (and Lambda'/Gamma' for l = 0, 1), leaves the eigenvectors in `vme`
 // (shared memory) for the overlap pass and, if `m_out` is given, the
@@ -47,14 +61,15 @@ __device__ __forceinline__ void prep_energy_layer(const OscParams& osc, double E
     const double fE = phase_rate_factor(E);
     const double k1 = (m[1] - m[0]) * fE;
     const double k2 = (m[2] - m[0]) * fE;
-    const size_t base = ((size_t)tile * g.nl + l) * W * te + lane;
+    const size_t block = ((size_t)tile * g.nl + l) * W * te;  // this (tile, layer)'s words
+    const size_t base = block + lane;
     if (MIXED) {
-        int* t = (int*)g.tab;
+        int* t = (int*)g.tab + block;
         const float k1h = f32_rn(k1), k2h = f32_rn(k2);
-        t[base + 9 * (size_t)te] = __float_as_int(k1h);
-        t[base + 10 * (size_t)te] = __float_as_int(f32_rn(k1 - f64_of(k1h)));
-        t[base + 11 * (size_t)te] = __float_as_int(k2h);
-        t[base + 12 * (size_t)te] = __float_as_int(f32_rn(k2 - f64_of(k2h)));
+        t[mixed_word_offset(9, lane, te)] = __float_as_int(k1h);
+        t[mixed_word_offset(10, lane, te)] = __float_as_int(f32_rn(k1 - f64_of(k1h)));
+        t[mixed_word_offset(11, lane, te)] = __float_as_int(k2h);
+        t[mixed_word_offset(12, lane, te)] = __float_as_int(f32_rn(k2 - f64_of(k2h)));
     } else {
         double* t = (double*)g.tab;
         t[base + 9 * (size_t)te] = k1;
@@ -93,7 +108,8 @@ __device__ __forceinline__ void prep_overlap_v(int l, int e, const GridTables& g
     const int te = g.te, tile = e / te, lane = e % te;
     const int W = MIXED ? kMixedWords : kFp64Words;
     if (!(check_ok(kSitePrepTab, tile, g.n_en_pad / te) && check_ok(kSitePrepLayer, l, g.nl))) return;
-    const size_t base = ((size_t)tile * g.nl + l) * W * te + lane;
+    const size_t block = ((size_t)tile * g.nl + l) * W * te;
+    const size_t base = block + lane;
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -101,7 +117,7 @@ __device__ __forceinline__ void prep_overlap_v(int l, int e, const GridTables& g
             const double tij = (l + 1 < g.nl) ? vn[i] * v[j] + vn[3 + i] * v[3 + j] + vn[6 + i] * v[6 + j]
                                               : (i == j ? 1.0 : 0.0);
             if (MIXED)
-                ((int*)g.tab)[base + (size_t)(3 * i + j) * te] = (l & 1) ? -q30_rn(tij) : q30_rn(tij);
+                ((int*)g.tab)[block + mixed_word_offset(3 * i + j, lane, te)] = (l & 1) ? -q30_rn(tij) : q30_rn(tij);
             else
                 ((double*)g.tab)[base + (size_t)(3 * i + j) * te] = tij;
         }
@@ -135,25 +151,37 @@ __device__ __forceinline__ void prep_cosine_layer(double cz, int M, const double
 // ------------------------------------------------------------ propagate ----
 template <int TE>
 struct MixedSrc {
-    const int* tab;    // shared: [nl][13][TE], offset by the thread's lane
-    const int* pe;     // shared: [18][TE], offset by lane
+    const int* tab;    // shared: the tile's [nl][13 words][TE] in the grouped layout (mixed_word_offset)
+    const int* pe;     // shared: [18 words][TE] in the grouped layout (mixed_pe_offset)
     const float2* len; // shared: this cosine's [nl_pad]
     const int4* ptab;  // shared: 257 (Q1.30 cos, sin, float cos, sin)
-    __device__ __forceinline__ int T(int l, int i, int j) const { return tab[(l * kMixedWords + 3 * i + j) * TE]; }
+    int lane;          // the thread's energy within the tile
+    static __device__ __forceinline__ int pick(int4 v, int c) { return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w; }
+    // word w of layer l: words 0-11 come from 16-byte loads (the compiler
+    // merges the loads of one group), word 12 from a 4-byte load
+    __device__ __forceinline__ int word(int l, int w) const {
+        if (w < 12) return pick(((const int4*)(tab + l * kMixedWords * TE))[(w >> 2) * TE + lane], w & 3);
+        return tab[l * kMixedWords * TE + 12 * TE + lane];
+    }
+    __device__ __forceinline__ int pe_word(int w) const {
+        if (w < 16) return pick(((const int4*)pe)[(w >> 2) * TE + lane], w & 3);
+        const int2 v = ((const int2*)(pe + 16 * TE))[lane];
+        return w == 16 ? v.x : v.y;
+    }
+    __device__ __forceinline__ int T(int l, int i, int j) const { return word(l, 3 * i + j); }
     // the chain over layers 1 .. M-1 crossed floor(M/2) negated overlaps
     __device__ __forceinline__ bool det_flip(int M) const { return (M >> 1) & 1; }
-    __device__ __forceinline__ int La(int j) const { return pe[j * TE]; }
-    __device__ __forceinline__ Q30::C Lb(int j) const { return Q30::C{pe[(3 + 2 * j) * TE], pe[(4 + 2 * j) * TE]}; }
-    __device__ __forceinline__ int Ga(int k) const { return pe[(9 + k) * TE]; }
-    __device__ __forceinline__ Q30::C Gb(int k) const { return Q30::C{pe[(12 + 2 * k) * TE], pe[(13 + 2 * k) * TE]}; }
+    __device__ __forceinline__ int La(int j) const { return pe_word(j); }
+    __device__ __forceinline__ Q30::C Lb(int j) const { return Q30::C{pe_word(3 + 2 * j), pe_word(4 + 2 * j)}; }
+    __device__ __forceinline__ int Ga(int k) const { return pe_word(9 + k); }
+    __device__ __forceinline__ Q30::C Gb(int k) const { return Q30::C{pe_word(12 + 2 * k), pe_word(13 + 2 * k)}; }
     __device__ __forceinline__ void phase(int l, int& c1, int& s1, int& n1, int& c2, int& s2, int& n2) const {
         phase_len(l, len[l], c1, s1, n1, c2, s2, n2);
     }
     __device__ __forceinline__ void phase_len(int l, float2 L, int& c1, int& s1, int& n1, int& c2, int& s2,
                                               int& n2) const {
-        const int* k = tab + (l * kMixedWords + 9) * TE;
-        phase_q30(__int_as_float(k[0]), __int_as_float(k[TE]), L.x, L.y, ptab, c1, s1);
-        phase_q30(__int_as_float(k[2 * TE]), __int_as_float(k[3 * TE]), L.x, L.y, ptab, c2, s2);
+        phase_q30(__int_as_float(word(l, 9)), __int_as_float(word(l, 10)), L.x, L.y, ptab, c1, s1);
+        phase_q30(__int_as_float(word(l, 11)), __int_as_float(word(l, 12)), L.x, L.y, ptab, c2, s2);
         n1 = -s1;
         n2 = -s2;
     }
@@ -161,10 +189,9 @@ struct MixedSrc {
     __device__ __forceinline__ void phase_acc(int l, int& c1, int& s1, int& n1, int& c2, int& s2, int& n2,
                                               Turns& acc) const {
         const float2 L = len[l];
-        const int* k = tab + (l * kMixedWords + 9) * TE;
         float p1, e1, p2, e2;
-        turns_product(__int_as_float(k[0]), __int_as_float(k[TE]), L.x, L.y, p1, e1);
-        turns_product(__int_as_float(k[2 * TE]), __int_as_float(k[3 * TE]), L.x, L.y, p2, e2);
+        turns_product(__int_as_float(word(l, 9)), __int_as_float(word(l, 10)), L.x, L.y, p1, e1);
+        turns_product(__int_as_float(word(l, 11)), __int_as_float(word(l, 12)), L.x, L.y, p2, e2);
         const float u1 = p1 - rintf(p1), u2 = p2 - rintf(p2);
         turns_q30_u(u1, e1, ptab, c1, s1);
         turns_q30_u(u2, e2, ptab, c2, s2);
@@ -379,7 +406,7 @@ __device__ __forceinline__ void process_tile(const TileJob& j, int nl, int nl_pa
         const Word* pe = (const Word*)j.pe;
         for (int i = t; i < kPerEWords * TE; i += nt) {
             const int w = i / TE, lane = i % TE;
-            s_pe[i] = pe[(size_t)w * j.n_en_pad + (size_t)j.etile * TE + lane];
+            s_pe[MIXED ? mixed_pe_offset(w, lane, TE) : i] = pe[(size_t)w * j.n_en_pad + (size_t)j.etile * TE + lane];
         }
         const int nlen16 = j.ncl * nl_pad / 2;  // 8-byte entries, nl_pad even
         block_copy16(s_len_raw, (const unsigned char*)j.len + (size_t)j.c0 * nl_pad * 8, nlen16);
@@ -405,8 +432,8 @@ __device__ __forceinline__ void process_tile(const TileJob& j, int nl, int nl_pa
         const int M = CP3_IX(kSiteTileLayers, s_maxl[cl], nl);
         const int ci = j.c0 + cl;
         if (MIXED) {
-            MixedSrc<TE> src{(const int*)s_tab + lane, (const int*)s_pe + lane,
-                             (const float2*)s_len_raw + (size_t)cl * nl_pad, s_ptab};
+            MixedSrc<TE> src{(const int*)s_tab, (const int*)s_pe, (const float2*)s_len_raw + (size_t)cl * nl_pad,
+                             s_ptab, lane};
             const Q30 ar{};
             float pr[9];
             if (MODE == kModeHeights) {
