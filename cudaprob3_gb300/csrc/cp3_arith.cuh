@@ -164,21 +164,42 @@ struct Q30 {
 // sin * 2^30: the corrections come out in Q1.30 units) for j = -128..128 at
 // index j + 128.  u lies in [-1/2, 1/2], so j = rint(256 u) is in range; a
 // NaN phase converts to j = 0.
+// rint(256 u) for |u| <= 1/2 by adding 1.5 * 2^23: the sum's last place is 1,
+// so the add rounds to the nearest integer with ties to even (as rintf does),
+// and the integer sits in the low bits of the sum's encoding
+// (kRoundOffsetBits + j), which also serves as the table index without a
+// float-to-int conversion.
+constexpr float kRoundOffset = 12582912.0f;  // 1.5 * 2^23
+constexpr int kRoundOffsetBits = 0x4B400000;
+
 // Q1.30 cos/sin of 2 pi (p + e) for a phase given in turns as a double-float
-// pair (|e| small against 1): steps 2-4 above.
-__device__ __forceinline__ void turns_q30_u(float u, float e, const int4* __restrict__ tab, int& cq, int& sq) {
-    const float j = rintf(u * 256.0f);
-    const float d = fmaf(j, -0.00390625f, u) + e;
+// pair (|e| small against 1): steps 2-4 above.  Also returns the encoding of
+// the offset sum (jbits, whose low 8 bits are j mod 256) and the remainder d,
+// from which the caller can sum phases (TurnSum).
+__device__ __forceinline__ void turns_q30_u(float u, float e, const int4* __restrict__ tab, int& cq, int& sq,
+                                            int& jbits, float& d) {
+    const float t = __fmaf_rn(u, 256.0f, kRoundOffset);
+    const float j = __fsub_rn(t, kRoundOffset);
+    d = fmaf(j, -0.00390625f, u) + e;
+    jbits = __float_as_int(t);
     // sin(2 pi d) and cos(2 pi d) - 1 with 2 pi folded into the coefficients
     const float d2 = d * d;
     const float sx = d * fmaf(d2, -4.134170224e+01f, 6.283185307e+00f);
     const float cm = d2 * fmaf(d2, 6.493939402e+01f, -1.973920880e+01f);
-    const int4 t = tab[CP3_IX(kSitePhaseTable, (int)j + 128, kPhaseTabN + 1)];
-    const float cf = __int_as_float(t.z), sf = __int_as_float(t.w);
+    // index j + 128 in [0, 256]; a NaN phase lands past the end and is held
+    // at the last entry (its d is NaN, so the result is NaN either way)
+    const unsigned ix = min((unsigned)(jbits - (kRoundOffsetBits - kPhaseTabN / 2)), (unsigned)kPhaseTabN);
+    const int4 t4 = tab[CP3_IX(kSitePhaseTable, (int)ix, kPhaseTabN + 1)];
+    const float cf = __int_as_float(t4.z), sf = __int_as_float(t4.w);
     const float dc = fmaf(cf, cm, -sf * sx);  // Q1.30 units
     const float ds = fmaf(sf, cm, cf * sx);
-    cq = t.x + __float2int_rn(dc);
-    sq = t.y + __float2int_rn(ds);
+    cq = t4.x + __float2int_rn(dc);
+    sq = t4.y + __float2int_rn(ds);
+}
+__device__ __forceinline__ void turns_q30_u(float u, float e, const int4* __restrict__ tab, int& cq, int& sq) {
+    int jbits;
+    float d;
+    turns_q30_u(u, e, tab, cq, sq, jbits, d);
 }
 __device__ __forceinline__ void turns_q30(float p, float e, const int4* __restrict__ tab, int& cq, int& sq) {
     turns_q30_u(p - rintf(p), e, tab, cq, sq);
@@ -202,16 +223,19 @@ __device__ __forceinline__ void phase_q30(float kh, float kl, float Lh, float Ll
 
 // Running sum of phases in turns as a Q0.32 fixed-point fraction: only
 // e^{2 pi i sum} is needed, so the sum is kept modulo one turn by the 32-bit
-// wrap-around.  Each phase adds its reduced part u (|u| <= 1/2) and its small
-// double-float remainder e, each rounded to 2^-32 turns.
+// wrap-around.  A phase t = integer + j/256 + d (turns_q30_u) adds j exactly
+// (as the low 8 bits of its offset encoding, summed apart and moved to bits
+// 24..31 at the end) and d rounded to 2^-32 turns.
 struct TurnSum {
-    unsigned acc = 0u;
-    __device__ __forceinline__ void add(float u, float e) {
-        acc += (unsigned)__float2int_rn(u * 4294967296.0f) + (unsigned)__float2int_rn(e * 4294967296.0f);
+    unsigned jsum = 0u;  // sum of jbits: low 8 bits are sum(j) mod 256
+    unsigned dsum = 0u;  // sum of round(d * 2^32)
+    __device__ __forceinline__ void add(int jbits, float d) {
+        jsum += (unsigned)jbits;
+        dsum += (unsigned)__float2int_rn(d * 4294967296.0f);
     }
     // the sum as a reduced float u in [-1/2, 1/2) and its exact remainder e
     __device__ __forceinline__ void split(float& u, float& e) const {
-        const int a = (int)acc;
+        const int a = (int)((jsum << 24) + dsum);
         u = (float)a * 2.3283064365386963e-10f;  // 2^-32
         e = (float)(a - __float2int_rn(u * 4294967296.0f)) * 2.3283064365386963e-10f;
     }

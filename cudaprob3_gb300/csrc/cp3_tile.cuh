@@ -193,10 +193,12 @@ struct MixedSrc {
         turns_product(__int_as_float(word(l, 9)), __int_as_float(word(l, 10)), L.x, L.y, p1, e1);
         turns_product(__int_as_float(word(l, 11)), __int_as_float(word(l, 12)), L.x, L.y, p2, e2);
         const float u1 = p1 - rintf(p1), u2 = p2 - rintf(p2);
-        turns_q30_u(u1, e1, ptab, c1, s1);
-        turns_q30_u(u2, e2, ptab, c2, s2);
-        acc.add(u1, e1);
-        acc.add(u2, e2);
+        int j1, j2;
+        float d1, d2;
+        turns_q30_u(u1, e1, ptab, c1, s1, j1, d1);
+        turns_q30_u(u2, e2, ptab, c2, s2, j2, d2);
+        acc.add(j1, d1);
+        acc.add(j2, d2);
         n1 = -s1;
         n2 = -s2;
     }
