@@ -32,6 +32,9 @@ struct Q30 {
     struct C {
         int re, im;
     };
+    // flavour_block's order (cp3_chain.cuh): through G = Y^T D_M Y, which
+    // frees Y before X' (no spill at the 64-register cap)
+    static constexpr bool kBlockByRows = false;
 
     static __device__ __forceinline__ long long mul(int a, int b) {
         long long d;
@@ -250,6 +253,8 @@ struct F64 {
     struct C {
         double re, im;
     };
+    // flavour_block's order (cp3_chain.cuh): by rows of Y, 9 products fewer
+    static constexpr bool kBlockByRows = true;
     static __device__ __forceinline__ R one() { return 1.0; }
     static __device__ __forceinline__ C cz() { return C{0.0, 0.0}; }
     static __device__ __forceinline__ C creal(R x) { return C{x, 0.0}; }

@@ -20,14 +20,13 @@
 
 namespace cp3 {
 
-// G = Y^T D_M Y (symmetric, entries 00 01 02 11 12 22) of a pair that
-// crosses M >= 1 shells, Y = T_{M-1} D_{M-1} ... T_1 D_1.
+// Y = T_{M-1} D_{M-1} ... T_1 D_1 (row-major, Y[3 i + j]) of a pair that
+// crosses M >= 1 shells.
 template <class P, class Src>
-__device__ __forceinline__ void chain_G(const P& ar, const Src& src, int M, typename P::C G[6]) {
+__device__ __forceinline__ void chain_Y(const P& ar, const Src& src, int M, typename P::C Y[9]) {
     using R = typename P::R;
     using C = typename P::C;
     R c1, s1, n1, c2, s2, n2;
-    C Y[9];
     if (M >= 2) {
         // Only columns 0 and 1 of Y are propagated; Y is unitary with
         // det Y = prod_l det(T_l) det(D_l) = e^{2 pi i sum_l (t1 + t2)_l}
@@ -75,7 +74,16 @@ __device__ __forceinline__ void chain_G(const P& ar, const Src& src, int M, type
         for (int i = 0; i < 9; i++) Y[i] = P::cz();
         Y[0] = Y[4] = Y[8] = P::creal(P::one());
     }
-    // G = Y^T D_M Y (symmetric)
+}
+
+// G = Y^T D_M Y (symmetric, entries 00 01 02 11 12 22) for the chain Y of
+// a pair that crosses M >= 1 shells.
+template <class P, class Src>
+__device__ __forceinline__ void gram_G(const P& ar, const Src& src, int M, const typename P::C Y[9],
+                                       typename P::C G[6]) {
+    using R = typename P::R;
+    using C = typename P::C;
+    R c1, s1, n1, c2, s2, n2;
     src.phase(M, c1, s1, n1, c2, s2, n2);
     {
         C Z[9];
@@ -91,6 +99,13 @@ __device__ __forceinline__ void chain_G(const P& ar, const Src& src, int M, type
 #pragma unroll
             for (int j = i; j < 3; j++) G[g++] = ar.dotCC(Y[i], Y[3 + i], Y[6 + i], Z[j], Z[3 + j], Z[6 + j]);
     }
+}
+
+template <class P, class Src>
+__device__ __forceinline__ void chain_G(const P& ar, const Src& src, int M, typename P::C G[6]) {
+    typename P::C Y[9];
+    chain_Y(ar, src, M, Y);
+    gram_G(ar, src, M, Y, G);
 }
 
 // Src provides, for the current pair:
@@ -112,11 +127,23 @@ template <class P, class Src>
 __device__ __forceinline__ void flavour_block(const P& ar, const Src& src, int M, typename P::C B[4]) {
     using R = typename P::R;
     using C = typename P::C;
-    // G = Y^T D_M Y first: nothing of the atmosphere segment is live during
-    // the layer chain (fewer registers across the loop)
-    C G[6];  // 00 01 02 11 12 22
-    if (M > 0) chain_G(ar, src, M, G);
-    // X' = T_0 D_0 Gamma' (3x2), or D_0 Gamma' when only the atmosphere is crossed
+    // The chain first: nothing of the atmosphere segment is live during the
+    // layer loop (fewer registers across it).  The block is
+    // Lambda' G X' with G = Y^T D_M Y and X' = T_0 D_0 Gamma' (3x2), formed in
+    // one of two orders (same products up to rounding):
+    //   G, then X = G X', then Lambda' X: 156 products after the chain; Y is
+    //     dead before X' is formed (the Q1.30 path: no spill at 64 registers);
+    //   by rows r_k of Y: a_k = Lambda' r_k, b_k = X'^T r_k and
+    //     block = sum_k d_k a_k b_k^T, each entry rounded once: 147 products,
+    //     but Y stays live beside X' (the FP64 path, which has the registers:
+    //     2 % faster there; 24 bytes of spill and no gain on the Q1.30 path).
+    constexpr bool by_rows = P::kBlockByRows;
+    C Y[9];
+    C G[6];  // 00 01 02 11 12 22 (first order only)
+    if (M > 0) {
+        chain_Y(ar, src, M, Y);
+        if constexpr (!by_rows) gram_G(ar, src, M, Y, G);
+    }
     R c1, s1, n1, c2, s2, n2;
     src.phase(0, c1, s1, n1, c2, s2, n2);
     C g0[3], g1[3];  // D_0 Gamma': columns 0 and 1
@@ -136,25 +163,49 @@ __device__ __forceinline__ void flavour_block(const P& ar, const Src& src, int M
         B[3] = ar.dotCC(b0, b1, b2, g1[0], g1[1], g1[2]);
         return;
     }
-    C x0[3], x1[3];  // T_0 (D_0 Gamma')
+    C x0[3], x1[3];  // X' = T_0 (D_0 Gamma')
 #pragma unroll
     for (int i = 0; i < 3; i++) {
         x0[i] = ar.dotRC(src.T(0, i, 0), src.T(0, i, 1), src.T(0, i, 2), g0[0], g0[1], g0[2]);
         x1[i] = ar.dotRC(src.T(0, i, 0), src.T(0, i, 1), src.T(0, i, 2), g1[0], g1[1], g1[2]);
     }
-    // X = G X' (3x2)
-    C X0[3], X1[3];
-    X0[0] = ar.dotCC(G[0], G[1], G[2], x0[0], x0[1], x0[2]);
-    X0[1] = ar.dotCC(G[1], G[3], G[4], x0[0], x0[1], x0[2]);
-    X0[2] = ar.dotCC(G[2], G[4], G[5], x0[0], x0[1], x0[2]);
-    X1[0] = ar.dotCC(G[0], G[1], G[2], x1[0], x1[1], x1[2]);
-    X1[1] = ar.dotCC(G[1], G[3], G[4], x1[0], x1[1], x1[2]);
-    X1[2] = ar.dotCC(G[2], G[4], G[5], x1[0], x1[1], x1[2]);
-    // block = Lambda' X: row 0 of W V_1 is real, row 1 complex
-    B[0] = ar.dotRC(src.La(0), src.La(1), src.La(2), X0[0], X0[1], X0[2]);
-    B[1] = ar.dotRC(src.La(0), src.La(1), src.La(2), X1[0], X1[1], X1[2]);
-    B[2] = ar.dotCC(src.Lb(0), src.Lb(1), src.Lb(2), X0[0], X0[1], X0[2]);
-    B[3] = ar.dotCC(src.Lb(0), src.Lb(1), src.Lb(2), X1[0], X1[1], X1[2]);
+    if constexpr (by_rows) {
+        // every factor is a dot product of unit vectors (|.| <= 1, as the
+        // Gauss products need); row 0 of W V_1 is real, row 1 complex
+        C a0[3], a1[3], b0[3], b1[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            b0[k] = ar.dotCC(Y[3 * k], Y[3 * k + 1], Y[3 * k + 2], x0[0], x0[1], x0[2]);
+            b1[k] = ar.dotCC(Y[3 * k], Y[3 * k + 1], Y[3 * k + 2], x1[0], x1[1], x1[2]);
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            a0[k] = ar.dotRC(src.La(0), src.La(1), src.La(2), Y[3 * k], Y[3 * k + 1], Y[3 * k + 2]);
+            a1[k] = ar.dotCC(src.Lb(0), src.Lb(1), src.Lb(2), Y[3 * k], Y[3 * k + 1], Y[3 * k + 2]);
+        }
+        src.phase(M, c1, s1, n1, c2, s2, n2);
+        a0[1] = ar.mulPhase(a0[1], c1, s1, n1);
+        a1[1] = ar.mulPhase(a1[1], c1, s1, n1);
+        a0[2] = ar.mulPhase(a0[2], c2, s2, n2);
+        a1[2] = ar.mulPhase(a1[2], c2, s2, n2);
+        B[0] = ar.dotCC(a0[0], a0[1], a0[2], b0[0], b0[1], b0[2]);
+        B[1] = ar.dotCC(a0[0], a0[1], a0[2], b1[0], b1[1], b1[2]);
+        B[2] = ar.dotCC(a1[0], a1[1], a1[2], b0[0], b0[1], b0[2]);
+        B[3] = ar.dotCC(a1[0], a1[1], a1[2], b1[0], b1[1], b1[2]);
+    } else {
+        // X = G X' (3x2), then the block = Lambda' X
+        C X0[3], X1[3];
+        X0[0] = ar.dotCC(G[0], G[1], G[2], x0[0], x0[1], x0[2]);
+        X0[1] = ar.dotCC(G[1], G[3], G[4], x0[0], x0[1], x0[2]);
+        X0[2] = ar.dotCC(G[2], G[4], G[5], x0[0], x0[1], x0[2]);
+        X1[0] = ar.dotCC(G[0], G[1], G[2], x1[0], x1[1], x1[2]);
+        X1[1] = ar.dotCC(G[1], G[3], G[4], x1[0], x1[1], x1[2]);
+        X1[2] = ar.dotCC(G[2], G[4], G[5], x1[0], x1[1], x1[2]);
+        B[0] = ar.dotRC(src.La(0), src.La(1), src.La(2), X0[0], X0[1], X0[2]);
+        B[1] = ar.dotRC(src.La(0), src.La(1), src.La(2), X1[0], X1[1], X1[2]);
+        B[2] = ar.dotCC(src.Lb(0), src.Lb(1), src.Lb(2), X0[0], X0[1], X0[2]);
+        B[3] = ar.dotCC(src.Lb(0), src.Lb(1), src.Lb(2), X1[0], X1[1], X1[2]);
+    }
 }
 
 // Probabilities of one pair averaged over production heights h with weights
