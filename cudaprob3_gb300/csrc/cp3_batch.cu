@@ -808,32 +808,21 @@ int cp3_batch_set_density(cp3_batch* b, const double* radii, const double* rhos,
     if (n <= 0) return bfail(CP3_ERR_ARGUMENT, "setDensity : vectors must not be empty");
     if (!radii || !rhos) return bfail(CP3_ERR_ARGUMENT, "setDensity : null array");
     if (n > CP3_MAX_ROWS) return bfail(CP3_ERR_LIMIT, "setDensity : more than 64 rows");
-    bool flip = false;
-    if (n >= 2) {
-        const int sign = (radii[1] - radii[0] > 0 ? 1 : -1);
-        for (int i = 1; i < n; i++)
-            if ((radii[i] - radii[i - 1]) * sign < 0) return bfail(CP3_ERR_ARGUMENT, "radii order messed up");
-        flip = sign == 1;
-    }
+    // the single-grid handle's ordering and checks (propagator.hpp:117-161)
+    cp3::BodyRow rows[CP3_MAX_ROWS];
+    if (const char* msg = cp3::order_body(radii, rhos, ye, n, rows)) return bfail(CP3_ERR_ARGUMENT, msg);
     for (int s = 0; scale && s < b->n_sets; s++)
         if (!(scale[s] >= 0.0) || !std::isfinite(scale[s]))
             return bfail(CP3_ERR_ARGUMENT, "batch: density scales must be finite and >= 0");
     b->radii.resize(n);
     b->rhos.resize(n);
     b->ye.resize(n);
-    for (int i = 0; i < n; i++) {
-        const int s = flip ? n - 1 - i : i;
-        if (!(radii[s] >= 0.0) || !(rhos[s] >= 0.0) || (ye && !(ye[s] >= 0.0 && ye[s] <= 1.0)))
-            return bfail(CP3_ERR_ARGUMENT, "setDensity : bad radius, density or electron fraction");
-        b->radii[i] = radii[s];
-        b->rhos[i] = rhos[s];
-        b->ye[i] = ye ? ye[s] : 0.5;
-    }
     b->coslimit.resize(n);
     for (int i = 0; i < n; i++) {
-        double x = -1 * std::sqrt(1 - (b->radii[i] * b->radii[i] / (cp3::kREarth * cp3::kREarth)));
-        if (i == 0) x = 0;
-        b->coslimit[i] = x;
+        b->radii[i] = rows[i].radius;
+        b->rhos[i] = rows[i].rho;
+        b->ye[i] = rows[i].ye;
+        b->coslimit[i] = rows[i].coslimit;
     }
     if (scale)
         b->scale.assign(scale, scale + b->n_sets);

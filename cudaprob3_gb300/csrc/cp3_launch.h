@@ -92,6 +92,7 @@ inline void fill_phase_table(bool mixed, int4* tab) {
 struct BodyRow {
     double radius, rho, ye;
     double coslimit;  // cosine below which a trajectory enters this shell
+    int row;          // the caller's index of this row
 };
 
 // Propagator::setDensity (propagator.hpp:117-161) for n >= 1 rows given in
@@ -118,6 +119,7 @@ inline const char* order_body(const double* radii, const double* rhos, const dou
         out[i].radius = radii[s];
         out[i].rho = rhos[s];
         out[i].ye = ye ? ye[s] : 0.5;
+        out[i].row = s;
         double x = -1 * std::sqrt(1 - (out[i].radius * out[i].radius / (kREarth * kREarth)));
         if (i == 0) x = 0;
         out[i].coslimit = x;

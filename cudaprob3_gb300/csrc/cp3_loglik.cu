@@ -1206,27 +1206,20 @@ int cp3_loglik_set_bins(cp3_loglik* L, const double* cosines, const double* ener
 int cp3_loglik_set_body(cp3_loglik* L, const double* radii, const double* ye, int n) {
     if (!L || !radii || n <= 0) return lfail(CP3_ERR_ARGUMENT, "setDensity : vectors must not be empty");
     if (n > CP3_MAX_ROWS) return lfail(CP3_ERR_LIMIT, "setDensity : more than 64 rows");
-    bool flip = false;
-    if (n >= 2) {
-        const int sign = (radii[1] - radii[0] > 0 ? 1 : -1);
-        for (int i = 1; i < n; i++)
-            if ((radii[i] - radii[i - 1]) * sign < 0) return lfail(CP3_ERR_ARGUMENT, "radii order messed up");
-        flip = sign == 1;
-    }
+    // the single-grid handle's ordering and checks (propagator.hpp:117-161);
+    // the densities are parameters of the evaluation, so none are given here
+    const double no_rhos[CP3_MAX_ROWS] = {};
+    cp3::BodyRow rows[CP3_MAX_ROWS];
+    if (const char* msg = cp3::order_body(radii, no_rhos, ye, n, rows)) return lfail(CP3_ERR_ARGUMENT, msg);
     L->radii.resize(n);
     L->ye.resize(n);
+    L->coslimit.resize(n);
     L->layer_row.assign(n + 1, -1);
     for (int i = 0; i < n; i++) {
-        const int s = flip ? n - 1 - i : i;
-        L->radii[i] = radii[s];
-        L->ye[i] = ye ? ye[s] : 0.5;
-        L->layer_row[i + 1] = s;
-    }
-    L->coslimit.resize(n);
-    for (int i = 0; i < n; i++) {
-        double x = -1 * std::sqrt(1 - (L->radii[i] * L->radii[i] / (cp3::kREarth * cp3::kREarth)));
-        if (i == 0) x = 0;
-        L->coslimit[i] = x;
+        L->radii[i] = rows[i].radius;
+        L->ye[i] = rows[i].ye;
+        L->coslimit[i] = rows[i].coslimit;
+        L->layer_row[i + 1] = rows[i].row;
     }
     L->n_rows = n;
     L->has_body = true;

@@ -286,10 +286,32 @@ CP3_HD void layer_eigen(const OscParams& p, double E, double rhoye, double m[3],
 // phase_rate_factor(E) * (m_k - m_0), the factor computed once per (energy, layer).
 CP3_HD double phase_rate_factor(double E) { return div_nr(-kLoEfac / kTwoPi, E); }
 
+// Products and differences rounded one at a time, as the reference's host
+// build evaluates the trajectory geometry (no fused multiply-add): near a
+// shell's tangent the chord's square root amplifies a one-ulp difference in
+// its argument (cosines one ulp from a shell boundary gave 1e-8 in P from
+// contracted products), so the lengths follow the reference's roundings.
+// Host builds of these helpers compile with -ffp-contract=off.
+CP3_HD double mul_rn(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __dmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+CP3_HD double sub_rn(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __dsub_rn(a, b);
+#else
+    return a - b;
+#endif
+}
+
 // Total path length including the production height (physics.hpp:615-616), cm.
 CP3_HD double path_length_cm(double c, double height_cm) {
     const double re = kREarth * kKm2Cm;
-    return sqrt((re + height_cm) * (re + height_cm) - (re * re) * (1.0 - c * c)) - re * c;
+    const double rh = re + height_cm;
+    return sub_rn(sqrt(sub_rn(mul_rn(rh, rh), mul_rn(re * re, sub_rn(1.0, mul_rn(c, c))))), mul_rn(re, c));
 }
 
 // Length in km of the segment of layer `l` (0 = atmosphere, 1..M shells from
@@ -304,14 +326,14 @@ CP3_HD double km_of_cm(double x) {
 
 CP3_HD double layer_length_km(const double* radii, int l, int M, double c, double path_cm) {
     if (c >= 0.0) return km_of_cm(path_cm);
-    const double earth_cm = -2.0 * c * (kREarth * kKm2Cm);
-    if (l == 0) return km_of_cm(path_cm - earth_cm);
+    const double earth_cm = mul_rn(-2.0 * c, kREarth * kKm2Cm);
+    if (l == 0) return km_of_cm(sub_rn(path_cm, earth_cm));
     const int i = l - 1;
-    const double perp2 = kREarth * kREarth * (1.0 - c * c);
-    double q = radii[i] * radii[i] - perp2;
+    const double perp2 = mul_rn(kREarth * kREarth, sub_rn(1.0, mul_rn(c, c)));
+    double q = sub_rn(mul_rn(radii[i], radii[i]), perp2);
     const double cross_this = 2.0 * sqrt(q > 0.0 ? q : 0.0);
     if (i < M - 1) {
-        double qn = radii[i + 1] * radii[i + 1] - perp2;
+        double qn = sub_rn(mul_rn(radii[i + 1], radii[i + 1]), perp2);
         const double cross_next = 2.0 * sqrt(qn > 0.0 ? qn : 0.0);
         return km_of_cm(0.5 * (cross_this - cross_next) * kKm2Cm);
     }

@@ -1,0 +1,120 @@
+"""Edge cases of the propagation against the oracle, both precisions:
+  * the largest body the handle takes (64 rows: 65 layers, so that the mixed
+    kernel halves its energy tile and cosine chunk to fit shared memory) and
+    the 65-row body it refuses;
+  * energies up to 1e6 GeV, where the matter term dominates and the phases
+    are small (the reference's own FP64 roots lose digits there: the oracle's
+    rows and columns sum to one only to ~6e-11, so FP64 is held to 2e-10
+    against it and to 1e-12 on its own unitarity);
+  * cosines exactly on the shell boundaries coslimit = -sqrt(1 - r^2/R^2)
+    (a trajectory tangent to a shell) and one ulp to either side, where the
+    layer count and the chord lengths switch (propagator.hpp:149-158,
+    301-307; physics.hpp:555-580);
+  * no mixing (all angles zero: the eigenvectors are the axes, P = identity),
+    maximal mixing, and a body of vacuum rows (zero density).
+Tolerances: FP64 1e-11 (2e-10 at the highest energies), mixed 1e-6."""
+import numpy as np
+import pytest
+
+import oracle
+from cudaprob3_gb300 import grids as G
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp64": 1e-11, "mixed": 1e-6}
+R_EARTH = 6371.0
+
+
+def run(gpu, precision, cos, en, radii, rhos, ye, params, anti=False, h=22.0):
+    with gpu.CudaPropagatorSingle(0, len(cos), len(en), precision=precision) as p:
+        p.setEnergyList(en)
+        p.setCosineList(cos)
+        p.setMNSMatrix(*params[:4])
+        p.setNeutrinoMasses(*params[4:])
+        p.setDensity(radii, rhos, ye)
+        p.setProductionHeight(h)
+        p.calculateProbabilities(gpu.Antineutrino if anti else gpu.Neutrino)
+        return p.results().astype(np.float64)
+
+
+def body_64():
+    rng = np.random.default_rng(5)
+    radii = np.concatenate([[0.0], np.sort(rng.uniform(10.0, R_EARTH - 10.0, 62)), [R_EARTH]])
+    rhos = np.sort(rng.uniform(1.0, 13.0, 64))[::-1].copy()
+    ye = np.where(radii <= 3480.0, 0.468, 0.497)
+    return G.Body(radii, rhos, ye)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("anti", [False, True])
+def test_largest_body(gpu, precision, anti):
+    B = body_64()
+    c, e = G.linspace(-1, 0.2, 67), G.logspace(0.1, 200, 75)
+    got = run(gpu, precision, c, e, B.radii, B.rhos, B.ye, G.NOMINAL, anti)
+    want = oracle.calculate(c, e, B.radii, B.rho_eff(), G.NOMINAL, 22.0, anti)
+    assert np.abs(got - want).max() <= TOL[precision]
+
+
+def test_body_above_the_row_limit_is_refused(gpu):
+    B = body_64()
+    radii = np.concatenate([[0.0], np.sort(np.append(B.radii[1:-1], 3000.5)), [R_EARTH]])
+    assert radii.size == 65
+    with gpu.CudaPropagatorSingle(0, 4, 4, precision="mixed") as p:
+        with pytest.raises(gpu.CP3Error, match="more than 64 rows"):
+            p.setDensity(radii, np.ones(65))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_highest_energies(gpu, precision):
+    B = G.PREM_12
+    c, e = G.linspace(-1, 0.2, 41), G.logspace(1e2, 1e6, 37)
+    for anti in (False, True):
+        got = run(gpu, precision, c, e, B.radii, B.rhos, B.ye, G.NOMINAL, anti)
+        want = oracle.calculate(c, e, B.radii, B.rho_eff(), G.NOMINAL, 22.0, anti)
+        tol = 2e-10 if precision == "fp64" else TOL[precision]
+        assert np.abs(got - want).max() <= tol
+        s = got.reshape(3, 3, c.size, e.size)
+        unit = 1e-12 if precision == "fp64" else 1e-6
+        assert np.abs(s.sum(axis=0) - 1).max() <= unit and np.abs(s.sum(axis=1) - 1).max() <= unit
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cosines_on_shell_boundaries(gpu, precision):
+    B = G.PREM_12
+    # the host's cosine limits (propagator.hpp:149-158), and one ulp either side
+    lim = -np.sqrt(1.0 - (B.radii * B.radii) / (R_EARTH * R_EARTH))
+    lim = lim[(lim > -1.0) & (lim < 0.0)]
+    c = np.clip(np.concatenate([lim, np.nextafter(lim, -2.0), np.nextafter(lim, 2.0), [-1.0, 0.0]]), -1.0, 1.0)
+    e = G.logspace(0.3, 80, 23)
+    # the layer counts follow the oracle's (strict c < coslimit)
+    with gpu.CudaPropagatorSingle(0, c.size, e.size, precision=precision) as p:
+        p.setEnergyList(e)
+        p.setCosineList(c)
+        p.setDensity(B.radii, B.rhos, B.ye)
+        assert np.array_equal(p.maxlayers(), oracle.maxlayers(c, B.radii))
+    for anti in (False, True):
+        got = run(gpu, precision, c, e, B.radii, B.rhos, B.ye, G.NOMINAL, anti)
+        want = oracle.calculate(c, e, B.radii, B.rho_eff(), G.NOMINAL, 22.0, anti)
+        assert np.abs(got - want).max() <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("case", ["no_mixing", "maximal_mixing", "vacuum_body"])
+def test_parameter_and_body_extremes(gpu, precision, case):
+    B = G.PREM_12
+    params, rhos = G.NOMINAL, B.rhos
+    if case == "no_mixing":
+        params = (0.0, 0.0, 0.0, 0.0) + tuple(G.NOMINAL[4:])
+    elif case == "maximal_mixing":
+        params = (np.pi / 4, np.pi / 4, np.pi / 4, np.pi / 2) + tuple(G.NOMINAL[4:])
+    else:
+        rhos = np.zeros_like(B.rhos)
+    c, e = G.linspace(-1, 1, 45), G.logspace(0.1, 300, 39)
+    for anti in (False, True):
+        got = run(gpu, precision, c, e, B.radii, rhos, B.ye, params, anti)
+        want = oracle.calculate(c, e, B.radii, rhos * B.ye / 0.5, params, 22.0, anti)
+        assert np.abs(got - want).max() <= TOL[precision], (case, anti)
+        if case == "no_mixing":
+            s = got.reshape(3, 3, c.size, e.size)
+            for k in range(3):
+                assert np.abs(s[k, k] - 1.0).max() <= TOL[precision]
