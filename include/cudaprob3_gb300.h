@@ -68,7 +68,7 @@ int cp3_abi_version(void);
  * its buffer's extent; a failure is recorded (never a trap), the access is
  * kept inside the buffer, and the wait that ends the calculation
  * (cp3_wait_for_completion, cp3_batch_wait, cp3_loglik_evaluate, and the
- * no-allocation call, which waits in this build) returns CP3_ERR_CHECK with
+ * no-allocation call, which waits in the checked build) returns CP3_ERR_CHECK with
  * the kernel, index and extent in cp3_last_error(). */
 int cp3_bounds_checked(void);
 

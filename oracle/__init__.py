@@ -1,4 +1,4 @@
-"""Oracle package: the checker for the CUDA library (test infrastructure only).
+"""Oracle package: the CPU oracle of the CUDA library (test infrastructure only).
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline and
 reference arms (the CPU port, and the reference's own kernel on the GPU)

@@ -1,7 +1,7 @@
 /*
  * Oracle: CPU restatement of CUDAProb3++'s CpuPropagator path (double and float).
  *
- * TEST INFRASTRUCTURE ONLY.  It is the checker for the CUDA library: only
+ * TEST INFRASTRUCTURE ONLY.  It is the oracle of the CUDA library: only
  * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference arm
  * load it.  The product path (cudaprob3_gb300) never links or calls it.
  *

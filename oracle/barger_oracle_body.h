@@ -1,7 +1,7 @@
 /*
  * Oracle body: CPU restatement of CUDAProb3++'s CpuPropagator<FLOAT_T> path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker used by tests/,
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle used by tests/,
  * __graft_entry__.smoke() and the CPU-baseline leg of bench.py.  The
  * product (cudaprob3_gb300) never links, imports or calls it.
  *

@@ -1,4 +1,4 @@
-// Checker-only loader of the reference's CUDA kernel (oracle/ref_gpu_kernel.cu,
+// Test-only loader of the reference's CUDA kernel (oracle/ref_gpu_kernel.cu,
 // compiled into oracle/_ref/ref_kernels.cubin) for bench.py's comparison with
 // the reference on the GPU.  It contains no physics: it loads the cubin, copies
 // the __constant__ data and the device arrays that the reference's own host

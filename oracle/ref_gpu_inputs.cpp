@@ -1,4 +1,4 @@
-// Checker-only: the host-side inputs of the reference's CUDA kernel for the
+// Test infrastructure only: the host-side inputs of the reference's CUDA kernel for the
 // 4096 x 4096 benchmark grid, produced by the reference's own host code.
 //
 // CudaPropagatorSingle::calculateProbabilitiesAsync (cudapropagator.cuh:191-220)

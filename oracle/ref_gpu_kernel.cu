@@ -1,11 +1,12 @@
-// Checker-only: the reference's own CUDA kernel, calculateKernel<FLOAT_T>
-// (physics.hpp:705-721, launched by CudaPropagatorSingle with 64-thread blocks
-// and SDIV(n_energies, 64) * n_cosines blocks, cudapropagator.cuh:191-220),
-// compiled from the reference's headers where they lie into a cubin for
-// sm_103a (oracle/Makefile, target refgpu; output oracle/_ref/, never
-// committed).  It is the comparison the survey names for the GPU: the
-// reference's kernel recompiled for this GPU.  Nothing in the product loads
-// it; bench.py times it through oracle/ref_gpu_driver.cpp.
+// Test infrastructure only: the reference's own CUDA kernel,
+// calculateKernel<FLOAT_T> (physics.hpp:705-721, launched by
+// CudaPropagatorSingle with 64-thread blocks and SDIV(n_energies, 64) *
+// n_cosines blocks, cudapropagator.cuh:191-220), compiled from the reference's
+// headers where they lie into a cubin for sm_103a (oracle/Makefile, target
+// refgpu; output oracle/_ref/, never committed): the reference's GPU path
+// recompiled for this GPU, the comparison for the propagation kernels on the
+// same device.  Nothing in the product loads it; bench.py times it through
+// oracle/ref_gpu_driver.cpp.
 // the include order of cudapropagator.cuh:23-26
 #include "constants.hpp"
 #include "propagator.hpp"

@@ -1,4 +1,4 @@
-// Checker-only shim: exposes the reference's own CpuPropagator<FLOAT_T>
+// Test-only shim: exposes the reference's own CpuPropagator<FLOAT_T>
 // (cpupropagator.hpp:34-108) through a flat C ABI so that Python can call it
 // to produce golden vectors.  It is compiled from the reference headers where
 // they lie (see oracle/Makefile) into oracle/_ref/, which is never committed.

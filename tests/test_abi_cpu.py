@@ -70,7 +70,7 @@ def product_files():
 
 
 def test_product_never_touches_the_oracle():
-    # the oracle is the checker of tests and the CPU legs of bench.py only
+    # the oracle serves the tests and the CPU legs of bench.py only
     hits = [p for p in product_files() if re.search(r"\boracle\b", open(p).read())]
     assert not hits, hits
 

@@ -20,7 +20,10 @@ def test_port_matches_reference_goldens(name):
     assert np.abs(sub - g["probs"]).max() <= 1e-12
 
 
-def test_survey_probe_values():
+def test_reference_probe_values():
+    """P(mu -> mu) of the reference's CpuPropagator<double> on the 4-shell body
+    (neutrinos, 256 x 256 grid) at cos = -1, E = 0.5 GeV and cos = 0,
+    E = 100 GeV, as a run of the reference printed them."""
     g = load_golden("prem4_256_ye05")
     ic = list(g["idx_c"])
     ie = list(g["idx_e"])
