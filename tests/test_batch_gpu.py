@@ -107,3 +107,14 @@ def test_batch_errors(gpu):
             b.calculate(0)
         with pytest.raises(CP3Error, match="unsupported launch shape"):
             b.set_launch_shape(48, 2, 8)
+        # the body goes through the single-grid handle's checks (propagator.hpp:117-161)
+        with pytest.raises(CP3Error, match="radii order messed up"):
+            b.set_density([0.0, 3000.0, 2000.0], [1.0, 1.0, 1.0])
+        with pytest.raises(CP3Error, match="must be finite"):
+            b.set_density([0.0, np.inf], [1.0, 1.0])
+        with pytest.raises(CP3Error, match="must be finite"):
+            b.set_density([0.0, 6371.0], [1.0, -1.0])
+        with pytest.raises(CP3Error, match="electron fractions"):
+            b.set_density([0.0, 6371.0], [1.0, 1.0], [0.5, 1.5])
+        with pytest.raises(CP3Error, match="more than 64 rows"):
+            b.set_density(np.linspace(0.0, 6371.0, 65), np.ones(65))

@@ -98,3 +98,12 @@ def test_loglik_errors(gpu):
     with LogLikelihood(0, 4, 5) as L:
         with pytest.raises(CP3Error, match="must be set"):
             L.evaluate(np.array(G.NOMINAL), np.ones(5))
+        # the body goes through the single-grid handle's checks (propagator.hpp:117-161)
+        with pytest.raises(CP3Error, match="radii order messed up"):
+            L.set_body([0.0, 3000.0, 2000.0])
+        with pytest.raises(CP3Error, match="must be finite"):
+            L.set_body([0.0, np.nan])
+        with pytest.raises(CP3Error, match="electron fractions"):
+            L.set_body([0.0, 6371.0], [0.5, -0.1])
+        with pytest.raises(CP3Error, match="more than 64 rows"):
+            L.set_body(np.linspace(0.0, 6371.0, 65))
