@@ -86,6 +86,7 @@ SIGNATURES = [
     ("cp3_batch_wait", _I, [_P]),
     ("cp3_batch_calculate_sequential", _I, [_P, _I]),
     ("cp3_batch_last_ms", _I, [_P, ctypes.POINTER(ctypes.c_float)]),
+    ("cp3_batch_launch_count", _I, [_P, _I, _IP]),
     ("cp3_batch_result_offsets", _I, [_P, ctypes.POINTER(ctypes.c_longlong)]),
     ("cp3_batch_result_device_ptr", _I, [_P, ctypes.POINTER(_P)]),
     ("cp3_batch_copy_results_to_host", _I, [_P, _P, _SZ]),
@@ -101,6 +102,7 @@ SIGNATURES = [
     ("cp3_loglik_set_kernel_timing", _I, [_P, _I]),
     ("cp3_loglik_last_kernel_ms", _I, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
                                        ctypes.POINTER(ctypes.c_float)]),
+    ("cp3_loglik_io_bytes", _I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
     ("cp3_propagate_noalloc", _I, [_I, _I, _P, _I, _P, _I, _DP, _DP, _DP, _I, _D, _D, _D, _D, _D, _D, _D, _P,
                                    _P]),
 ]

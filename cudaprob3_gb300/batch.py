@@ -122,6 +122,12 @@ class BatchPropagator:
         check(self._lib.cp3_batch_last_ms(self._h, ctypes.byref(ms)))
         return ms.value
 
+    def launch_count(self, ntype=0):
+        """Kernels one calculate() launches (prep and propagate of every chunk)."""
+        n = ctypes.c_int()
+        check(self._lib.cp3_batch_launch_count(self._h, int(ntype), ctypes.byref(n)))
+        return n.value
+
     def result_device_ptr(self):
         p = ctypes.c_void_p()
         check(self._lib.cp3_batch_result_device_ptr(self._h, ctypes.byref(p)))

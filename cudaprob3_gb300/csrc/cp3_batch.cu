@@ -963,6 +963,17 @@ int cp3_batch_last_ms(cp3_batch* b, float* ms) {
     return CP3_OK;
 }
 
+int cp3_batch_launch_count(cp3_batch* b, int type, int* launches) {
+    if (!b || !launches) return bfail(CP3_ERR_ARGUMENT, "null argument");
+    Guard g(b->device);
+    if (g.err) return bcuda(g.err, "cudaSetDevice");
+    if (int rc = ready(b, type)) return rc;  // the layout the graph is captured from
+    int n = b->n_chunks;                      // one prep launch per chunk
+    for (int k = 0; k < b->n_chunks; k++) n += (b->chunk_items[k + 1] > b->chunk_items[k]);
+    *launches = n;
+    return CP3_OK;
+}
+
 int cp3_batch_result_offsets(cp3_batch* b, long long* offsets) {
     if (!b || !offsets) return bfail(CP3_ERR_ARGUMENT, "null argument");
     std::copy(b->out_off.begin(), b->out_off.end(), offsets);

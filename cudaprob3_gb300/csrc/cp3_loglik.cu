@@ -1350,4 +1350,14 @@ int cp3_loglik_last_kernel_ms(cp3_loglik* L, float* prep_ms, float* pair_ms, flo
     return CP3_OK;
 }
 
+int cp3_loglik_io_bytes(cp3_loglik* L, long long* host_to_device, long long* device_to_host) {
+    if (!L) return lfail(CP3_ERR_ARGUMENT, "null argument");
+    if (!L->has_body) return lfail(CP3_ERR_STATE, "loglik_io_bytes: the body is not set");
+    // the graph's parameter copy (cp3_loglik_evaluate fills kOscBlock and one
+    // rho*Ye per layer) and the rows the layer kernel writes
+    if (host_to_device) *host_to_device = (long long)(kOscBlock + sizeof(double) * (L->n_rows + 1));
+    if (device_to_host) *device_to_host = (long long)sizeof(double) * L->n_en * (7 + L->n_rows);
+    return CP3_OK;
+}
+
 }  // extern "C"

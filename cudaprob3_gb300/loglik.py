@@ -95,6 +95,12 @@ class LogLikelihood:
         check(self._lib.cp3_loglik_last_kernel_ms(self._h, *[ctypes.byref(x) for x in t]))
         return tuple(x.value for x in t)
 
+    def io_bytes(self):
+        """(host-to-device, device-to-host) bytes of one evaluation."""
+        up, down = ctypes.c_longlong(), ctypes.c_longlong()
+        check(self._lib.cp3_loglik_io_bytes(self._h, ctypes.byref(up), ctypes.byref(down)))
+        return up.value, down.value
+
 
 class BinnedProblem:
     """The inputs of a binned fit (see the module docstring)."""

@@ -270,6 +270,9 @@ int cp3_batch_wait(cp3_batch* b);
 int cp3_batch_calculate_sequential(cp3_batch* b, int type);
 /* device time of the last calculation (events around the graph or launches) */
 int cp3_batch_last_ms(cp3_batch* b, float* ms);
+/* kernels one cp3_batch_calculate launches (the graph's prep and propagate
+ * launches of every chunk, for the current sets and launch shape) */
+int cp3_batch_launch_count(cp3_batch* b, int type, int* launches);
 /* n_sets + 1 element offsets of each set's planes in the result buffer */
 int cp3_batch_result_offsets(cp3_batch* b, long long* offsets);
 int cp3_batch_result_device_ptr(cp3_batch* b, void** dptr);
@@ -306,6 +309,10 @@ int cp3_loglik_evaluate(cp3_loglik* L, int type, const double* params, const dou
  * the last evaluation. */
 int cp3_loglik_set_kernel_timing(cp3_loglik* L, int enable);
 int cp3_loglik_last_kernel_ms(cp3_loglik* L, float* prep_ms, float* pair_ms, float* layer_ms);
+/* Bytes one evaluation moves between host and device: the parameter block
+ * the graph uploads, and the per-energy log-likelihood and gradient rows the
+ * layer kernel writes into mapped host memory (the body must be set). */
+int cp3_loglik_io_bytes(cp3_loglik* L, long long* host_to_device, long long* device_to_host);
 
 /* ------------------------------------------------------------- no allocation
  * One calculation that allocates nothing.  No counterpart in the reference.
