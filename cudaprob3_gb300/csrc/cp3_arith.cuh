@@ -113,6 +113,20 @@ struct Q30 {
         gauss(a1, b0, r1, i1);
         return C{rnd(r0 - r1), rnd(i1 - i0)};
     }
+    // a b (|a|, |b| <= 1), one rounding
+    __device__ __forceinline__ C mulCC(C a, C b) const {
+        long long re, im;
+        gauss(a, b, re, im);
+        return C{rnd(re), rnd(im)};
+    }
+    // q0 + q1 e^{i psi1} + q2 e^{i psi2} (|q_k| <= 1), the rotations by
+    // Gauss's three products as in mulPhase, all summed exactly, one rounding
+    __device__ __forceinline__ C phaseSum(C q0, C q1, C q2, int c1, int s1, int c2, int s2) const {
+        const long long k1 = mul(c1, q1.re + q1.im), k2 = mul(c2, q2.re + q2.im);
+        const long long re = ((long long)q0.re << 30) + (k1 - mul(q1.im, c1 + s1)) + (k2 - mul(q2.im, c2 + s2));
+        const long long im = ((long long)q0.im << 30) + (k1 + mul(q1.re, s1 - c1)) + (k2 + mul(q2.re, s2 - c2));
+        return C{rnd(re), rnd(im)};
+    }
     // |z|^2 exactly, as Q2.60 in 64 bits
     static __device__ __forceinline__ long long norm2(C z) { return mul(z.re, z.re) + mul(z.im, z.im); }
     // Q2.60 probability -> float, one rounding; the completed entries of the
@@ -262,6 +276,11 @@ struct F64 {
     static __device__ __forceinline__ C mulRC(R t, C z) { return C{t * z.re, t * z.im}; }
     static __device__ __forceinline__ C mulCC(C a, C b) {
         return C{fma(a.re, b.re, -a.im * b.im), fma(a.re, b.im, a.im * b.re)};
+    }
+    // q0 + q1 e^{i psi1} + q2 e^{i psi2}
+    static __device__ __forceinline__ C phaseSum(C q0, C q1, C q2, double c1, double s1, double c2, double s2) {
+        return C{q0.re + fma(q1.re, c1, -q1.im * s1) + fma(q2.re, c2, -q2.im * s2),
+                 q0.im + fma(q1.im, c1, q1.re * s1) + fma(q2.im, c2, q2.re * s2)};
     }
     static __device__ __forceinline__ C mulPhase(C z, double c, double s, double /*ns*/) {
         return C{fma(z.re, c, -z.im * s), fma(z.im, c, z.re * s)};

@@ -212,7 +212,7 @@ __device__ __forceinline__ void flavour_block(const P& ar, const Src& src, int M
 // w_h (sum 1).  Only the atmosphere segment depends on h (physics.hpp:613-616),
 // so the block factors as B(h) = R D_0(h) Gamma' with R = Lambda' G T_0 (or
 // Gamma'^dagger when no shell is crossed): the chain runs once, each height
-// costs one phase pair and a 2x3 by 3x2 product.  `lenh` holds the pair's
+// costs one phase pair and four phase sums.  `lenh` holds the pair's
 // atmosphere length at every height in the Src's length format; the averaged
 // |B|^2 are completed to the nine probabilities (the completion is linear).
 template <class P, class Src, class LenT, class WT>
@@ -246,22 +246,28 @@ __device__ __forceinline__ void flavour_probs_heights(const P& ar, const Src& sr
             R1[k] = ar.dotRC(src.T(0, 0, k), src.T(0, 1, k), src.T(0, 2, k), l1[0], l1[1], l1[2]);
         }
     }
+    // B(h)[r][c] = sum_k R_r[k] d_k(h) Gamma'_c[k] = sum_k Q_rc[k] d_k(h) with
+    // d_0 = 1: the products Q_rc[k] = R_r[k] Gamma'_c[k] do not depend on the
+    // height (30 products once per pair), so a height costs two phases and
+    // four phase sums (24 products) instead of forming D_0(h) Gamma' and
+    // four 3-term dot products (46)
+    C Q00[3], Q01[3], Q10[3], Q11[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        Q00[k] = ar.mulRC(src.Ga(k), R0[k]);
+        Q01[k] = ar.mulCC(R0[k], src.Gb(k));
+        Q10[k] = ar.mulRC(src.Ga(k), R1[k]);
+        Q11[k] = ar.mulCC(R1[k], src.Gb(k));
+    }
     A q00 = 0, q01 = 0, q10 = 0, q11 = 0;
     for (int h = 0; h < H; h++) {
         R c1, s1, n1, c2, s2, n2;
         src.phase_len(0, lenh[h], c1, s1, n1, c2, s2, n2);
-        C g0[3], g1[3];  // D_0(h) Gamma'
-        g0[0] = P::creal(src.Ga(0));
-        g0[1] = ar.mulRC(src.Ga(1), C{c1, s1});
-        g0[2] = ar.mulRC(src.Ga(2), C{c2, s2});
-        g1[0] = src.Gb(0);
-        g1[1] = ar.mulPhase(src.Gb(1), c1, s1, n1);
-        g1[2] = ar.mulPhase(src.Gb(2), c2, s2, n2);
         const A wh = (A)w[h];
-        q00 += wh * P::prob(ar.dotCC(R0[0], R0[1], R0[2], g0[0], g0[1], g0[2]));
-        q01 += wh * P::prob(ar.dotCC(R0[0], R0[1], R0[2], g1[0], g1[1], g1[2]));
-        q10 += wh * P::prob(ar.dotCC(R1[0], R1[1], R1[2], g0[0], g0[1], g0[2]));
-        q11 += wh * P::prob(ar.dotCC(R1[0], R1[1], R1[2], g1[0], g1[1], g1[2]));
+        q00 += wh * P::prob(ar.phaseSum(Q00[0], Q00[1], Q00[2], c1, s1, c2, s2));
+        q01 += wh * P::prob(ar.phaseSum(Q01[0], Q01[1], Q01[2], c1, s1, c2, s2));
+        q10 += wh * P::prob(ar.phaseSum(Q10[0], Q10[1], Q10[2], c1, s1, c2, s2));
+        q11 += wh * P::prob(ar.phaseSum(Q11[0], Q11[1], Q11[2], c1, s1, c2, s2));
     }
     P::complete_avg(q00, q01, q10, q11, out);
 }
