@@ -51,7 +51,18 @@ struct OscParams {
     double ca, cb0, cb1, cg;  // cubic coefficients a = fac + ca, b = cb0 + fac cb1, g = fac cg
     double s23, c23, sd, cd;
     int anti;            // 1 for antineutrinos: sign of the matter term flips
+    // double-float (hi, lo) splits of the constants above, for the FP32-pipe
+    // eigen-solve of the mixed prep (cp3_physics.cuh layer_eigen_df)
+    float ca_f[2], cb0_f[2], cb1_f[2], cg_f[2];
+    float hv_f[6][2];
+    float s23_f[2], c23_f[2], sd_f[2], cd_f[2];
 };
+
+// hi = x rounded to float, lo = the rest rounded to float (a double-float split)
+inline void split_df(double x, float out[2]) {
+    out[0] = (float)x;
+    out[1] = (float)(x - (double)out[0]);
+}
 
 // OscParams from the six parameters (mixing angles and dcp in radians,
 // dm21 = m2^2 - m1^2 and dm32 = m3^2 - m2^2 in eV^2): the degeneracy break of
@@ -86,6 +97,15 @@ inline void fill_osc_params(OscParams& o, double th12, double th13, double th23,
     o.sd = std::sin(dcp);
     o.cd = std::cos(dcp);
     o.anti = anti ? 1 : 0;
+    split_df(o.ca, o.ca_f);
+    split_df(o.cb0, o.cb0_f);
+    split_df(o.cb1, o.cb1_f);
+    split_df(o.cg, o.cg_f);
+    for (int k = 0; k < 6; k++) split_df(o.hv[k], o.hv_f[k]);
+    split_df(o.s23, o.s23_f);
+    split_df(o.c23, o.c23_f);
+    split_df(o.sd, o.sd_f);
+    split_df(o.cd, o.cd_f);
 }
 
 // One problem for the kernels (device pointers).

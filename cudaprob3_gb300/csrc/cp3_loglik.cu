@@ -182,36 +182,78 @@ __global__ void __launch_bounds__(256) ll_prep_kernel(LLArgs a) {
         const int e = blockIdx.x * eb + ey;
         const bool live = (l < nl) && (e < a.n_en_pad);
         double* vme = s_v + ((size_t)ey * nl + (l < nl ? l : 0)) * 9;
-        if (live) {
-            const double E = a.energies[e < a.n_en ? e : a.n_en - 1];
-            double* ev = a.eig + ((size_t)e * nl + l) * kLLEigWords;
-            prep_energy_layer<false>(*a.osc, E, a.rhoye[l], l, e, g, vme, ev + 9);
-#pragma unroll
-            for (int q = 0; q < 9; q++) ev[q] = vme[q];
-        }
-        __syncthreads();
-        if (live) prep_overlap<false>(l, e, g, vme);
         if (a.tabf) {
-            // float shadow of this (energy, layer)'s words; thread l = 0 also
-            // converts the energy's Lambda' / Gamma' (written by l = 0 and 1)
-            __syncthreads();
-            if (live) {
-                const int tile = e / kLLTile, ln = e % kLLTile;
-                const double* t = a.tab + ((size_t)tile * nl + l) * kFp64Words * kLLTile + ln;
-                float* f = a.tabf + ((size_t)tile * nl + l) * kLLFWords * kLLTile + ln;
+            // mixed: the double-float eigen-solve (FP32 pipes) writes the float
+            // tables the pair kernel reads (T and Lambda'/Gamma' rounded to
+            // float, kappa as hi/lo) and the eigen-pairs of the layer kernel;
+            // the eigenvectors reach the overlap pass through shared memory as
+            // double-float pairs
+            const int tile = e / kLLTile, ln = e % kLLTile;
+            const bool ok = live && check_ok(kSiteLLPrep, tile, a.n_en_pad / kLLTile);
+            float* f = a.tabf + ((size_t)tile * nl + (l < nl ? l : 0)) * kLLFWords * kLLTile + ln;
+            if (ok) {
+                const double E = a.energies[e < a.n_en ? e : a.n_en - 1];
+                const DF Ed = df_from_double(E);
+                DF m[3], V[9];
+                layer_eigen_df(*a.osc, Ed, df_from_double(a.rhoye[l]), m, V);
+                double* ev = a.eig + ((size_t)e * nl + l) * kLLEigWords;
 #pragma unroll
-                for (int q = 0; q < 9; q++) f[q * kLLTile] = f32_rn(t[q * kLLTile]);
-#pragma unroll
-                for (int k = 0; k < 2; k++) {
-                    const double kd = t[(9 + k) * kLLTile];
-                    const float kh = f32_rn(kd);
-                    f[(9 + 2 * k) * kLLTile] = kh;
-                    f[(10 + 2 * k) * kLLTile] = f32_rn(kd - f64_of(kh));
+                for (int q = 0; q < 9; q++) {
+                    ev[q] = df_to_double(V[q]);
+                    df_store(vme + q, V[q]);
                 }
-                // the energy's 18 words, spread over its layers' threads
-                for (int w = l; w < 18; w += nl)
-                    a.pef[(size_t)w * a.n_en_pad + e] = f32_rn(a.pe[(size_t)w * a.n_en_pad + e]);
+#pragma unroll
+                for (int k = 0; k < 3; k++) ev[9 + k] = df_to_double(m[k]);
+                const DF fE = df_rate_factor(Ed);
+                const DF k1 = df_mul(df_sub(m[1], m[0]), fE), k2 = df_mul(df_sub(m[2], m[0]), fE);
+                f[9 * kLLTile] = k1.hi;
+                f[10 * kLLTile] = k1.lo;
+                f[11 * kLLTile] = k2.hi;
+                f[12 * kLLTile] = k2.lo;
+                if (l <= 1) {
+                    // Gamma' = columns e, mu of V_0^T W^dagger (l = 0), Lambda' =
+                    // rows e, mu of W V_1 (l = 1), W = R23 diag(1, 1, e^{i dcp})
+                    const DF c23 = df_load(a.osc->c23_f), s23 = df_load(a.osc->s23_f);
+                    const DF s23cd = df_mul(s23, df_load(a.osc->cd_f));
+                    DF s23sd = df_mul(s23, df_load(a.osc->sd_f));
+                    if (l == 0) s23sd = df_neg(s23sd);
+                    const int off = (l == 0) ? 9 : 0;
+#pragma unroll
+                    for (int k = 0; k < 3; k++) {
+                        a.pef[(size_t)(off + k) * a.n_en_pad + e] = V[k].hi;
+                        a.pef[(size_t)(off + 3 + 2 * k) * a.n_en_pad + e] =
+                            df_add(df_mul(c23, V[3 + k]), df_mul(s23cd, V[6 + k])).hi;
+                        a.pef[(size_t)(off + 4 + 2 * k) * a.n_en_pad + e] = df_mul(s23sd, V[6 + k]).hi;
+                    }
+                }
             }
+            __syncthreads();
+            if (ok) {
+                // T_l = V_{l+1}^T V_l (the identity for the innermost layer)
+                const bool last = !(l + 1 < nl);
+#pragma unroll
+                for (int i = 0; i < 3; i++)
+#pragma unroll
+                    for (int j = 0; j < 3; j++) {
+                        float t = (i == j) ? 1.0f : 0.0f;
+                        if (!last)
+                            t = df_add(df_add(df_mul(df_read(vme + 9 + i), df_read(vme + j)),
+                                              df_mul(df_read(vme + 12 + i), df_read(vme + 3 + j))),
+                                       df_mul(df_read(vme + 15 + i), df_read(vme + 6 + j)))
+                                    .hi;
+                        f[(3 * i + j) * kLLTile] = t;
+                    }
+            }
+        } else {
+            if (live) {
+                const double E = a.energies[e < a.n_en ? e : a.n_en - 1];
+                double* ev = a.eig + ((size_t)e * nl + l) * kLLEigWords;
+                prep_energy_layer<false>(*a.osc, E, a.rhoye[l], l, e, g, vme, ev + 9);
+#pragma unroll
+                for (int q = 0; q < 9; q++) ev[q] = vme[q];
+            }
+            __syncthreads();
+            if (live) prep_overlap<false>(l, e, g, vme);
         }
     } else {
         // one thread per (cosine, layer)

@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "cp3_df.cuh"
 #include "cp3_internal.h"
 
 #ifndef CP3_HD
@@ -285,6 +286,171 @@ CP3_HD void layer_eigen(const OscParams& p, double E, double rhoye, double m[3],
 // per-layer common phase of m_0 removed; in turns per km that is
 // phase_rate_factor(E) * (m_k - m_0), the factor computed once per (energy, layer).
 CP3_HD double phase_rate_factor(double E) { return div_nr(-kLoEfac / kTwoPi, E); }
+
+// ------------------------------------------------ double-float eigen-solve --
+// layer_eigen in double-float arithmetic (cp3_df.cuh) for the mixed prep,
+// whose outputs are Q1.30 words and float hi/lo pairs: the same steps (the
+// FP32 trigonometric first guess, Newton on the most isolated root,
+// deflation, projector columns of the two most isolated roots, the third
+// vector as their cross product), on the FP32 pipes instead of FP64.
+
+// double-float split of a double (one FP64 subtraction)
+CP3_HD DF df_from_double(double x) {
+    const float h = f32_rn(x);
+    return DF{h, f32_rn(x - f64_of(h))};
+}
+CP3_HD DF df_load(const float p[2]) { return DF{p[0], p[1]}; }
+
+constexpr float kGF_hi = (float)kGF;
+constexpr float kGF_lo = (float)(kGF - (double)(float)kGF);
+constexpr double kRate = -kLoEfac / kTwoPi;  // phase_rate_factor(E) * E
+constexpr float kRate_hi = (float)kRate;
+constexpr float kRate_lo = (float)(kRate - (double)(float)kRate);
+
+CP3_HD DF df_rate_factor(DF E) { return df_div(DF{kRate_hi, kRate_lo}, E); }
+
+CP3_HD DF cubic_newton_df(DF x, DF a, DF b, DF g) {
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        // p(x) = ((x + a) x + b) x + g in double-float; p'(x) in FP32 (the
+        // step's error is then quadratic plus 1e-7 times linear)
+        const DF p = df_add(df_mul(df_add(df_mul(df_add(x, a), x), b), x), g);
+        const float dp = f_fma(f_fma(3.0f, x.hi, f_add(a.hi, a.hi)), x.hi, b.hi);
+        if (dp != 0.0f) x = df_sub(x, df_mulf(p, f_div(1.0f, dp)));
+    }
+    return x;
+}
+
+// column of (H - ma)(H - mb) with the largest diagonal entry (projector_column)
+CP3_HD void projector_column_df(const DF H[9], DF ma, DF mb, DF c[3]) {
+    const DF a0 = df_sub(H[0], ma), a4 = df_sub(H[4], ma), a8 = df_sub(H[8], ma);
+    const DF b0 = df_sub(H[0], mb), b4 = df_sub(H[4], mb), b8 = df_sub(H[8], mb);
+    // the choice of column only needs the magnitudes: FP32
+    const float h1 = H[1].hi, h2 = H[2].hi, h5 = H[5].hi;
+    const float n00 = fabsf(f_fma(a0.hi, b0.hi, f_fma(h1, h1, f_mul(h2, h2))));
+    const float n11 = fabsf(f_fma(a4.hi, b4.hi, f_fma(h1, h1, f_mul(h5, h5))));
+    const float n22 = fabsf(f_fma(a8.hi, b8.hi, f_fma(h2, h2, f_mul(h5, h5))));
+    const int p = (n00 >= n11 && n00 >= n22) ? 0 : (n11 >= n22) ? 1 : 2;
+    const DF x0 = (p == 0) ? b0 : (p == 1) ? H[1] : H[2];
+    const DF x1 = (p == 1) ? b4 : (p == 0) ? H[1] : H[5];
+    const DF x2 = (p == 2) ? b8 : (p == 0) ? H[2] : H[5];
+    c[0] = df_add(df_add(df_mul(a0, x0), df_mul(H[1], x1)), df_mul(H[2], x2));
+    c[1] = df_add(df_add(df_mul(H[1], x0), df_mul(a4, x1)), df_mul(H[5], x2));
+    c[2] = df_add(df_add(df_mul(H[2], x0), df_mul(H[5], x1)), df_mul(a8, x2));
+}
+
+CP3_HD bool negative_largest_df(const DF c[3]) {
+    float big = c[0].hi;
+    if (fabsf(c[1].hi) > fabsf(big)) big = c[1].hi;
+    if (fabsf(c[2].hi) > fabsf(big)) big = c[2].hi;
+    return big < 0.0f;
+}
+
+CP3_HD DF df_dot3(const DF x[3], const DF y[3]) {
+    return df_add(df_add(df_mul(x[0], y[0]), df_mul(x[1], y[1])), df_mul(x[2], y[2]));
+}
+
+CP3_HD void layer_eigen_df(const OscParams& p, DF E, DF rhoye, DF m[3], DF V[9]) {
+    // matter term and the cubic's coefficients (physics.hpp:277-295)
+    DF fac = df_mul(df_mul(DF{kGF_hi, kGF_lo}, E), rhoye);
+    if (!p.anti) fac = df_neg(fac);
+    const DF a = df_add(fac, df_load(p.ca_f));
+    const DF b = df_add(df_mul(fac, df_load(p.cb1_f)), df_load(p.cb0_f));
+    const DF g = df_mul(fac, df_load(p.cg_f));
+    // physics.hpp:298-324: FP32 first guess of the trigonometric roots (a^2 - 3b
+    // and the numerator cancel: formed in double-float), then Newton
+    const DF a2 = df_mul(a, a);
+    DF tmp = df_sub(a2, df_mulf(b, 3.0f));
+    if (tmp.hi < 0.0f) tmp = DF{0.0f, 0.0f};
+    const float tmpf = tmp.hi;
+    const float sqf = f_sqrt(tmpf);
+    const DF num = df_add(df_sub(df_mulf(df_mul(a2, a), 2.0f), df_mulf(df_mul(a, b), 9.0f)), df_mulf(g, 27.0f));
+    float arg = num.hi / (2.0f * sqf * tmpf);
+    if (!(fabsf(arg) <= 1.0f)) arg = (arg > 0.0f) ? 1.0f : -1.0f;
+    const float th = acosf(arg) * (1.0f / 3.0f);
+    float sf, cf;
+#ifdef __CUDA_ARCH__
+    sincosf(th, &sf, &cf);
+#else
+    sf = std::sin(th);
+    cf = std::cos(th);
+#endif
+    const float hf = 0.866025403784438647f;  // sin(2pi/3)
+    const float ampf = -(2.0f / 3.0f) * sqf;
+    const float shf = a.hi * (-1.0f / 3.0f);
+    const float q0 = ampf * cf + shf;
+    const float q1 = ampf * (-0.5f * cf + hf * sf) + shf;
+    const float q2 = ampf * (-0.5f * cf - hf * sf) + shf;
+    // refine the most isolated root, deflate for the other two (layer_eigen)
+    const float d01 = fabsf(q0 - q1), d02 = fabsf(q0 - q2), d12 = fabsf(q1 - q2);
+    const float e0 = fminf(d01, d02), e1 = fminf(d01, d12), e2 = fminf(d02, d12);
+    const int ri = (e0 >= e1 && e0 >= e2) ? 0 : (e1 >= e2) ? 1 : 2;
+    const int rj = (ri == 2) ? 0 : ri + 1, rk = (ri == 0) ? 2 : ri - 1;
+    const float qi = (ri == 0) ? q0 : (ri == 1) ? q1 : q2;
+    const float qj = (rj == 0) ? q0 : (rj == 1) ? q1 : q2;
+    const float qk = (rk == 0) ? q0 : (rk == 1) ? q1 : q2;
+    const float ej = (rj == 0) ? e0 : (rj == 1) ? e1 : e2;
+    const float ek = (rk == 0) ? e0 : (rk == 1) ? e1 : e2;
+    const DF mi = cubic_newton_df(DF{qi, 0.0f}, a, b, g);
+    const DF S = df_neg(df_add(a, mi));
+    const DF P = (fabsf(qi) >= fabsf(qj) && fabsf(qi) >= fabsf(qk) && df_nonzero(mi)) ? df_neg(df_div(g, mi))
+                                                                                       : df_sub(b, df_mul(mi, S));
+    DF disc = df_sub(df_mul(S, S), df_mulf(P, 4.0f));
+    if (disc.hi < 0.0f) disc = DF{0.0f, 0.0f};
+    const DF root = df_sqrt(disc);
+    const DF big = df_mulf(df_add(S, (S.hi < 0.0f) ? df_neg(root) : root), 0.5f);
+    const DF small = df_nonzero(big) ? df_div(P, big) : DF{0.0f, 0.0f};
+    const bool big_lo = df_less(big, small);
+    const DF hi = big_lo ? small : big, lo = big_lo ? big : small;
+    const DF mj = (qj >= qk) ? hi : lo;
+    const DF mk = (qj >= qk) ? lo : hi;
+    m[0] = (ri == 0) ? mi : (rj == 0) ? mj : mk;
+    m[1] = (ri == 1) ? mi : (rj == 1) ? mj : mk;
+    m[2] = (ri == 2) ? mi : (rj == 2) ? mj : mk;
+
+    // H_r = O diag(0, d1, d2) O^T - fac e0 e0^T
+    const DF hv0 = df_load(p.hv_f[0]), hv1 = df_load(p.hv_f[1]), hv2 = df_load(p.hv_f[2]);
+    const DF hv3 = df_load(p.hv_f[3]), hv4 = df_load(p.hv_f[4]), hv5 = df_load(p.hv_f[5]);
+    const DF H[9] = {df_sub(hv0, fac), hv1, hv2, hv1, hv3, hv4, hv2, hv4, hv5};
+    const bool cyc = ej >= ek;
+    const int i = ri, j = cyc ? rj : rk;
+    const DF mje = cyc ? mj : mk, mke = cyc ? mk : mj;
+    DF vi[3], vj[3], vk[3];
+    projector_column_df(H, mje, mke, vi);
+    projector_column_df(H, mke, mi, vj);
+    {
+        const DF n2 = df_dot3(vi, vi);
+        DF inv = df_nonzero(n2) ? df_rsqrt(n2) : DF{0.0f, 0.0f};
+        if (negative_largest_df(vi)) inv = df_neg(inv);
+        for (int r = 0; r < 3; r++) vi[r] = df_mul(vi[r], inv);
+    }
+    const bool neg_j = negative_largest_df(vj);
+    const DF d = df_dot3(vj, vi);
+    for (int r = 0; r < 3; r++) vj[r] = df_sub(vj[r], df_mul(d, vi[r]));
+    {
+        const DF n2 = df_dot3(vj, vj);
+        DF inv = df_nonzero(n2) ? df_rsqrt(n2) : DF{0.0f, 0.0f};
+        if (neg_j) inv = df_neg(inv);
+        for (int r = 0; r < 3; r++) vj[r] = df_mul(vj[r], inv);
+    }
+    // (i, j, k) cyclic: v_k = v_i x v_j; otherwise v_k = v_j x v_i
+    vk[0] = df_sub(df_mul(vi[1], vj[2]), df_mul(vi[2], vj[1]));
+    vk[1] = df_sub(df_mul(vi[2], vj[0]), df_mul(vi[0], vj[2]));
+    vk[2] = df_sub(df_mul(vi[0], vj[1]), df_mul(vi[1], vj[0]));
+    if (!cyc)
+        for (int r = 0; r < 3; r++) vk[r] = df_neg(vk[r]);
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) V[3 * r + c] = (c == i) ? vi[r] : (c == j) ? vj[r] : vk[r];
+}
+
+// round((x.hi + x.lo) 2^30) for |x| < 2: the scaled high part is rounded
+// exactly in FP32, the rest added as a small float
+CP3_HD int q30_df(DF x) {
+    const float h = f_mul(x.hi, 1073741824.0f);
+    const float rh = rintf(h);
+    const float r = f_add(f_sub(h, rh), f_mul(x.lo, 1073741824.0f));
+    return (int)rh + (int)rintf(r);
+}
 
 // Products and differences rounded one at a time, as the reference's host
 // build evaluates the trajectory geometry (no fused multiply-add): near a

@@ -46,63 +46,80 @@ __host__ __device__ inline int mixed_pe_offset(int w, int lane, int te) {
 // Thread (l, e) of the energy part: eigen-solve of layer l at energy E, writes
 // kappa (and Lambda'/Gamma' for l = 0, 1), leaves the eigenvectors in `vme`
 // (shared memory) for the overlap pass and, if `m_out` is given, the
-// eigenvalues there.
+// eigenvalues there.  The mixed tables (Q1.30 words, float hi/lo pairs) come
+// from the double-float solve on the FP32 pipes (layer_eigen_df), and `vme`
+// then holds the eigenvectors as double-float pairs in the same 8-byte
+// slots; the FP64 tables from the FP64 solve.
 template <bool MIXED>
 __device__ __forceinline__ void prep_energy_layer(const OscParams& osc, double E, double rhoye, int l, int e,
                                                   const GridTables& g, double* vme, double* m_out = nullptr) {
     const int te = g.te, tile = e / te, lane = e % te;
     const int W = MIXED ? kMixedWords : kFp64Words;
     if (!(check_ok(kSitePrepTab, tile, g.n_en_pad / te) && check_ok(kSitePrepLayer, l, g.nl))) return;
-    double m[3], V[9];
-    layer_eigen(osc, E, rhoye, m, V);
-    for (int w = 0; w < 9; w++) vme[w] = V[w];
-    if (m_out)
-        for (int k = 0; k < 3; k++) m_out[k] = m[k];
-    const double fE = phase_rate_factor(E);
-    const double k1 = (m[1] - m[0]) * fE;
-    const double k2 = (m[2] - m[0]) * fE;
     const size_t block = ((size_t)tile * g.nl + l) * W * te;  // this (tile, layer)'s words
     const size_t base = block + lane;
-    if (MIXED) {
+    if constexpr (MIXED) {
+        const DF Ed = df_from_double(E);
+        DF m[3], V[9];
+        layer_eigen_df(osc, Ed, df_from_double(rhoye), m, V);
+        for (int w = 0; w < 9; w++) df_store(vme + w, V[w]);
+        if (m_out)
+            for (int k = 0; k < 3; k++) m_out[k] = df_to_double(m[k]);
+        const DF fE = df_rate_factor(Ed);
+        const DF k1 = df_mul(df_sub(m[1], m[0]), fE);
+        const DF k2 = df_mul(df_sub(m[2], m[0]), fE);
         int* t = (int*)g.tab + block;
-        const float k1h = f32_rn(k1), k2h = f32_rn(k2);
-        t[mixed_word_offset(9, lane, te)] = __float_as_int(k1h);
-        t[mixed_word_offset(10, lane, te)] = __float_as_int(f32_rn(k1 - f64_of(k1h)));
-        t[mixed_word_offset(11, lane, te)] = __float_as_int(k2h);
-        t[mixed_word_offset(12, lane, te)] = __float_as_int(f32_rn(k2 - f64_of(k2h)));
-    } else {
-        double* t = (double*)g.tab;
-        t[base + 9 * (size_t)te] = k1;
-        t[base + 10 * (size_t)te] = k2;
-    }
-    if (l <= 1) {
-        // per energy: Gamma' = columns e, mu of V_0^T W^dagger (l = 0) and
-        // Lambda' = rows e, mu of W V_1 (l = 1), W = R23 diag(1, 1, e^{i dcp})
-        const double sg = (l == 0) ? -1.0 : 1.0;  // e^{-i dcp} for Gamma', e^{+i dcp} for Lambda'
-        double w[9];
-        for (int k = 0; k < 3; k++) {
-            w[k] = V[k];
-            w[3 + 2 * k] = osc.c23 * V[3 + k] + osc.s23 * osc.cd * V[6 + k];
-            w[4 + 2 * k] = sg * osc.s23 * osc.sd * V[6 + k];
+        t[mixed_word_offset(9, lane, te)] = __float_as_int(k1.hi);
+        t[mixed_word_offset(10, lane, te)] = __float_as_int(k1.lo);
+        t[mixed_word_offset(11, lane, te)] = __float_as_int(k2.hi);
+        t[mixed_word_offset(12, lane, te)] = __float_as_int(k2.lo);
+        if (l <= 1) {
+            // per energy: Gamma' = columns e, mu of V_0^T W^dagger (l = 0) and
+            // Lambda' = rows e, mu of W V_1 (l = 1), W = R23 diag(1, 1, e^{i dcp})
+            const DF c23 = df_load(osc.c23_f), s23 = df_load(osc.s23_f);
+            const DF s23cd = df_mul(s23, df_load(osc.cd_f));
+            DF s23sd = df_mul(s23, df_load(osc.sd_f));
+            if (l == 0) s23sd = df_neg(s23sd);  // e^{-i dcp} for Gamma', e^{+i dcp} for Lambda'
+            int w[9];
+            for (int k = 0; k < 3; k++) {
+                w[k] = q30_df(V[k]);
+                w[3 + 2 * k] = q30_df(df_add(df_mul(c23, V[3 + k]), df_mul(s23cd, V[6 + k])));
+                w[4 + 2 * k] = q30_df(df_mul(s23sd, V[6 + k]));
+            }
+            const int off = (l == 0) ? 9 : 0;
+            for (int q = 0; q < 9; q++) ((int*)g.pe)[(size_t)(off + q) * g.n_en_pad + e] = w[q];
         }
-        const int off = (l == 0) ? 9 : 0;
-        for (int q = 0; q < 9; q++) {
-            const size_t idx = (size_t)(off + q) * g.n_en_pad + e;
-            if (MIXED)
-                ((int*)g.pe)[idx] = q30_rn(w[q]);
-            else
-                ((double*)g.pe)[idx] = w[q];
+    } else {
+        double m[3], V[9];
+        layer_eigen(osc, E, rhoye, m, V);
+        for (int w = 0; w < 9; w++) vme[w] = V[w];
+        if (m_out)
+            for (int k = 0; k < 3; k++) m_out[k] = m[k];
+        const double fE = phase_rate_factor(E);
+        double* t = (double*)g.tab;
+        t[base + 9 * (size_t)te] = (m[1] - m[0]) * fE;
+        t[base + 10 * (size_t)te] = (m[2] - m[0]) * fE;
+        if (l <= 1) {
+            const double sg = (l == 0) ? -1.0 : 1.0;
+            double w[9];
+            for (int k = 0; k < 3; k++) {
+                w[k] = V[k];
+                w[3 + 2 * k] = osc.c23 * V[3 + k] + osc.s23 * osc.cd * V[6 + k];
+                w[4 + 2 * k] = sg * osc.s23 * osc.sd * V[6 + k];
+            }
+            const int off = (l == 0) ? 9 : 0;
+            for (int q = 0; q < 9; q++) ((double*)g.pe)[(size_t)(off + q) * g.n_en_pad + e] = w[q];
         }
     }
 }
 
 // Overlap pass of thread (l, e): T_l = V_{l+1}^T V_l from its own eigenvectors
-// v and the next layer's vn; the innermost layer has no successor and keeps
-// the identity.  The mixed tables hold -T_l for odd l: the Q1.30 chain
-// rounds down (floor), and with the sign of Y alternating from layer to layer
-// the rounding errors of consecutive layers point in opposite directions in
-// the true frame instead of adding up (MixedSrc::det_flip restores the sign of
-// the third column).
+// v and the next layer's vn (double-float pairs for the mixed tables); the
+// innermost layer has no successor and keeps the identity.  The mixed tables
+// hold -T_l for odd l: the Q1.30 chain rounds down (floor), and with the sign
+// of Y alternating from layer to layer the rounding errors of consecutive
+// layers point in opposite directions in the true frame instead of adding up
+// (MixedSrc::det_flip restores the sign of the third column).
 template <bool MIXED>
 __device__ __forceinline__ void prep_overlap_v(int l, int e, const GridTables& g, const double* v, const double* vn) {
     const int te = g.te, tile = e / te, lane = e % te;
@@ -110,16 +127,22 @@ __device__ __forceinline__ void prep_overlap_v(int l, int e, const GridTables& g
     if (!(check_ok(kSitePrepTab, tile, g.n_en_pad / te) && check_ok(kSitePrepLayer, l, g.nl))) return;
     const size_t block = ((size_t)tile * g.nl + l) * W * te;
     const size_t base = block + lane;
+    const bool last = !(l + 1 < g.nl);
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
         for (int j = 0; j < 3; j++) {
-            const double tij = (l + 1 < g.nl) ? vn[i] * v[j] + vn[3 + i] * v[3 + j] + vn[6 + i] * v[6 + j]
-                                              : (i == j ? 1.0 : 0.0);
-            if (MIXED)
-                ((int*)g.tab)[block + mixed_word_offset(3 * i + j, lane, te)] = (l & 1) ? -q30_rn(tij) : q30_rn(tij);
-            else
+            if constexpr (MIXED) {
+                const DF tij = last ? DF{(i == j) ? 1.0f : 0.0f, 0.0f}
+                                    : df_add(df_add(df_mul(df_read(vn + i), df_read(v + j)),
+                                                    df_mul(df_read(vn + 3 + i), df_read(v + 3 + j))),
+                                             df_mul(df_read(vn + 6 + i), df_read(v + 6 + j)));
+                const int q = q30_df(tij);
+                ((int*)g.tab)[block + mixed_word_offset(3 * i + j, lane, te)] = (l & 1) ? -q : q;
+            } else {
+                const double tij = last ? (i == j ? 1.0 : 0.0) : vn[i] * v[j] + vn[3 + i] * v[3 + j] + vn[6 + i] * v[6 + j];
                 ((double*)g.tab)[base + (size_t)(3 * i + j) * te] = tij;
+            }
         }
 }
 
