@@ -91,12 +91,25 @@ CP3_HD DF two_prod(float a, float b) {
 }
 
 CP3_HD DF df_of(float a) { return DF{a, 0.0f}; }
-// a double-float pair kept in (or read from) an 8-byte double slot, bit for bit
-CP3_HD void df_store(double* slot, DF x) { memcpy(slot, &x, sizeof x); }
+// a double-float pair kept in (or read from) an 8-byte double slot, bit for
+// bit (hi in the high word); register moves only on the device
+CP3_HD void df_store(double* slot, DF x) {
+#ifdef __CUDA_ARCH__
+    *slot = __hiloint2double(__float_as_int(x.hi), __float_as_int(x.lo));
+#else
+    const float w[2] = {x.lo, x.hi};
+    memcpy(slot, w, sizeof w);
+#endif
+}
 CP3_HD DF df_read(const double* slot) {
-    DF x;
-    memcpy(&x, slot, sizeof x);
-    return x;
+#ifdef __CUDA_ARCH__
+    const double d = *slot;
+    return DF{__int_as_float(__double2hiint(d)), __int_as_float(__double2loint(d))};
+#else
+    float w[2];
+    memcpy(w, slot, sizeof w);
+    return DF{w[1], w[0]};
+#endif
 }
 CP3_HD DF df_neg(DF x) { return DF{-x.hi, -x.lo}; }
 CP3_HD double df_to_double(DF x) { return (double)x.hi + (double)x.lo; }

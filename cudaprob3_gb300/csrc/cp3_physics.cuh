@@ -422,15 +422,18 @@ CP3_HD void layer_eigen_df(const OscParams& p, DF E, DF rhoye, DF m[3], DF V[9])
         const DF n2 = df_dot3(vi, vi);
         DF inv = df_nonzero(n2) ? df_rsqrt(n2) : DF{0.0f, 0.0f};
         if (negative_largest_df(vi)) inv = df_neg(inv);
+#pragma unroll
         for (int r = 0; r < 3; r++) vi[r] = df_mul(vi[r], inv);
     }
     const bool neg_j = negative_largest_df(vj);
     const DF d = df_dot3(vj, vi);
+#pragma unroll
     for (int r = 0; r < 3; r++) vj[r] = df_sub(vj[r], df_mul(d, vi[r]));
     {
         const DF n2 = df_dot3(vj, vj);
         DF inv = df_nonzero(n2) ? df_rsqrt(n2) : DF{0.0f, 0.0f};
         if (neg_j) inv = df_neg(inv);
+#pragma unroll
         for (int r = 0; r < 3; r++) vj[r] = df_mul(vj[r], inv);
     }
     // (i, j, k) cyclic: v_k = v_i x v_j; otherwise v_k = v_j x v_i
@@ -438,8 +441,11 @@ CP3_HD void layer_eigen_df(const OscParams& p, DF E, DF rhoye, DF m[3], DF V[9])
     vk[1] = df_sub(df_mul(vi[2], vj[0]), df_mul(vi[0], vj[2]));
     vk[2] = df_sub(df_mul(vi[0], vj[1]), df_mul(vi[1], vj[0]));
     if (!cyc)
+#pragma unroll
         for (int r = 0; r < 3; r++) vk[r] = df_neg(vk[r]);
+#pragma unroll
     for (int r = 0; r < 3; r++)
+#pragma unroll
         for (int c = 0; c < 3; c++) V[3 * r + c] = (c == i) ? vi[r] : (c == j) ? vj[r] : vk[r];
 }
 

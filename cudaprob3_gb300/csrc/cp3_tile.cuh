@@ -62,8 +62,10 @@ __device__ __forceinline__ void prep_energy_layer(const OscParams& osc, double E
         const DF Ed = df_from_double(E);
         DF m[3], V[9];
         layer_eigen_df(osc, Ed, df_from_double(rhoye), m, V);
+#pragma unroll
         for (int w = 0; w < 9; w++) df_store(vme + w, V[w]);
         if (m_out)
+#pragma unroll
             for (int k = 0; k < 3; k++) m_out[k] = df_to_double(m[k]);
         const DF fE = df_rate_factor(Ed);
         const DF k1 = df_mul(df_sub(m[1], m[0]), fE);
@@ -81,12 +83,14 @@ __device__ __forceinline__ void prep_energy_layer(const OscParams& osc, double E
             DF s23sd = df_mul(s23, df_load(osc.sd_f));
             if (l == 0) s23sd = df_neg(s23sd);  // e^{-i dcp} for Gamma', e^{+i dcp} for Lambda'
             int w[9];
+#pragma unroll
             for (int k = 0; k < 3; k++) {
                 w[k] = q30_df(V[k]);
                 w[3 + 2 * k] = q30_df(df_add(df_mul(c23, V[3 + k]), df_mul(s23cd, V[6 + k])));
                 w[4 + 2 * k] = q30_df(df_mul(s23sd, V[6 + k]));
             }
             const int off = (l == 0) ? 9 : 0;
+#pragma unroll
             for (int q = 0; q < 9; q++) ((int*)g.pe)[(size_t)(off + q) * g.n_en_pad + e] = w[q];
         }
     } else {
