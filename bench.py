@@ -8,7 +8,7 @@ electron fractions 0.468 (core) / 0.497 (mantle), nominal oscillation point,
 production height 22 km, computed for neutrinos AND antineutrinos (two
 calculateProbabilities calls, 2 x 16.8M pairs).  Metric: (cos, E) pairs/s.
 
-Our arm runs the mixed-precision kernel (FP64 eigen-solve, Q1.30 fixed-point
+Our arm runs the mixed-precision kernel (double-float eigen-solve, Q1.30 fixed-point
 chain, float results) and reports beside it the plain FP64 kernel on the same
 workload, the precision of mixed against FP64 (every pair) and against the
 oracle (strided subset), the roofline of the dominant kernel and the CPU
@@ -659,7 +659,7 @@ def run_ours(args, world, rank, local):
         line = {
             "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "i32 Q1.30 chain + f32 phases + f64 eigen-solve (float out)",
+            "vs_baseline": None, "dtype": "i32 Q1.30 chain + f32 phases + double-float eigen-solve (float out)",
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "precision": "mixed", "pairs_per_step": pairs_step,
                        "l2": "flushed between steps (256 MB write outside the timed events); "
@@ -776,7 +776,7 @@ def run_batch(args, world, rank, local):
                           "launch (mixed)" % n,
                 "value": world * pairs / (ms * 1e-3), "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "i32 Q1.30 chain + f32 phases + f64 eigen-solve (float out)",
+                "vs_baseline": None, "dtype": "i32 Q1.30 chain + f32 phases + double-float eigen-solve (float out)",
                 "data": "synthetic",
                 "config": {"workload": "%d sets, cosines U{64..1024} in [-1,0], energies U{64..2048} over "
                                        "0.5-100 GeV, density scale U(0.97,1.03), seeds 0 (parameters) and 3 "
@@ -883,7 +883,7 @@ def run_rates(args, world, rank, local):
                 "value": world * pairs_step / (ms * 1e-3), "unit": "pairs/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
-                "dtype": "i32 Q1.30 chain + f32 phases + f64 eigen-solve, f32 run sums, f64 histograms",
+                "dtype": "i32 Q1.30 chain + f32 phases + double-float eigen-solve, f32 run sums, f64 histograms",
                 "data": "synthetic",
                 "config": {"workload": WORKLOAD + "; rates into 400 cos x 200 E bins, flux E^-2.7, nu_e = nu_mu/2",
                            "pairs_per_step": pairs_step,
@@ -972,7 +972,7 @@ def run_heights(args, world, rank, local):
                 "value": world * pairs_step / (ms * 1e-3), "unit": "pairs/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
-                "dtype": "i32 Q1.30 chain + f32 phases + f64 eigen-solve, f32 height sums (float out)",
+                "dtype": "i32 Q1.30 chain + f32 phases + double-float eigen-solve, f32 height sums (float out)",
                 "data": "synthetic",
                 "config": {"workload": WORKLOAD + "; heights 10-45 km (8), weights " +
                            ",".join("%.2f" % x for x in weights), "pairs_per_step": pairs_step,
@@ -1191,7 +1191,7 @@ def run_gradient(args, world, rank, local):
                 "value": world * out["mixed"]["evals_per_s"], "unit": "evaluations/s", "higher_is_better": True,
                 "n_gpus": world, "steps": out["mixed"]["evaluations"], "warmup": max(3, args.warmup),
                 "ms_per_step": out["mixed"]["ms_per_eval"], "scaling": "weak", "vs_baseline": None,
-                "dtype": "f32 pair kernel (double-float phases) + f64 eigen-solves and back-propagation",
+                "dtype": "f32 pair kernel (double-float phases) + double-float eigen-solves + f64 back-propagation",
                 "data": "synthetic", "clocks": out["mixed"]["clocks"],
                 "gpu_launches": 3 * out["mixed"]["evaluations"],
                 "e2e": {"value": world * out["mixed"]["evals_per_s"], "unit": "evaluations/s",

@@ -1,7 +1,8 @@
 // Per-tile and per-thread device code shared by the single-grid kernels
 // (cp3_kernels.cu) and the batched persistent kernel (cp3_batch.cu).
 //
-//   prep_energy_layer  FP64 eigen-solve of one (energy, layer) and the
+//   prep_energy_layer  eigen-solve of one (energy, layer) (double-float for
+//                      the mixed tables, FP64 for the FP64 ones) and the
 //                      mixed/FP64 table entries derived from it
 //   prep_overlap(_v)   T_l = V_{l+1}^T V_l of one (energy, layer)
 //   prep_cosine_layer  segment length of one (trajectory, layer)

@@ -4,8 +4,8 @@
 behaviour of cudaprob3::CudaPropagatorSingle<FLOAT_T> (cudapropagator.cuh:39-251)
 and its base cudaprob3::Propagator<FLOAT_T> (propagator.hpp:43-337); every call
 goes through the C ABI of libcudaprob3_gb300.so.  ``precision`` plays the role
-of FLOAT_T: "fp64" is the plain FP64 method (double results), "mixed" the FP64
-eigen-solve / 32-bit bulk method (float results).
+of FLOAT_T: "fp64" is the plain FP64 method (double results), "mixed" the
+double-float eigen-solve / 32-bit bulk method (float results).
 """
 import ctypes
 import enum

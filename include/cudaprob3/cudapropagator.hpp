@@ -2,7 +2,7 @@
 // over the C ABI: drop-ins for cudapropagator.cuh:39-251 and 258-458.
 //
 // FLOAT_T = double runs the plain FP64 kernel and returns doubles;
-// FLOAT_T = float runs the mixed kernel (FP64 eigen-solve, Q1.30 fixed-point
+// FLOAT_T = float runs the mixed kernel (double-float eigen-solve, Q1.30 fixed-point
 // chain, max |dP| <= 1e-6 against FP64) and returns floats.
 // Unlike the reference, each object owns its parameters (no process-global
 // constant memory), so objects with different parameters may coexist.

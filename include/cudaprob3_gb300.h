@@ -48,7 +48,7 @@ extern "C" {
 
 /* arithmetic of a propagator */
 #define CP3_PRECISION_FP64 0  /* plain method: every step in FP64              */
-#define CP3_PRECISION_MIXED 1 /* FP64 eigen-solve, 32-bit bulk, float results */
+#define CP3_PRECISION_MIXED 1 /* double-float eigen-solve, 32-bit bulk, float results */
 
 /* NeutrinoType, types.hpp:29 */
 #define CP3_NEUTRINO 0
