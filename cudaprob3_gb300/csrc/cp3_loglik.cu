@@ -72,6 +72,34 @@ template <class T>
 __device__ __forceinline__ Cx<T> cjmul(Cx<T> a, Cx<T> b) {
     return Cx<T>{a.re * b.re + a.im * b.im, a.re * b.im - a.im * b.re};
 }
+// a b + c, fused (one rounding), in the kernel's precision
+__device__ __forceinline__ float fm(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fm(double a, double b, double c) { return __fma_rn(a, b, c); }
+// s + conj(a) b as four fused multiply-adds
+template <class T>
+__device__ __forceinline__ Cx<T> cjmac(Cx<T> s, Cx<T> a, Cx<T> b) {
+    return Cx<T>{fm(a.im, b.im, fm(a.re, b.re, s.re)), fm(-a.im, b.re, fm(a.re, b.im, s.im))};
+}
+// s + a b as four fused multiply-adds
+template <class T>
+__device__ __forceinline__ Cx<T> cmac(Cx<T> s, Cx<T> a, Cx<T> b) {
+    return Cx<T>{fm(-a.im, b.im, fm(a.re, b.re, s.re)), fm(a.im, b.re, fm(a.re, b.im, s.im))};
+}
+// Re(conj(a0) b0 + conj(a1) b1 + conj(a2) b2) as one chain of multiply-adds
+template <class T>
+__device__ __forceinline__ T cjdot3_re(Cx<T> a0, Cx<T> b0, Cx<T> a1, Cx<T> b1, Cx<T> a2, Cx<T> b2) {
+    T s = a0.re * b0.re;
+    s = fm(a0.im, b0.im, s);
+    s = fm(a1.re, b1.re, s);
+    s = fm(a1.im, b1.im, s);
+    s = fm(a2.re, b2.re, s);
+    return fm(a2.im, b2.im, s);
+}
+// t0 z0 + t1 z1 + t2 z2 for real t as chains of multiply-adds
+template <class T>
+__device__ __forceinline__ Cx<T> rdot3(T t0, Cx<T> z0, T t1, Cx<T> z1, T t2, Cx<T> z2) {
+    return Cx<T>{fm(t2, z2.re, fm(t1, z1.re, t0 * z0.re)), fm(t2, z2.im, fm(t1, z1.im, t0 * z0.im))};
+}
 
 // One halving step of a many-value warp sum: lanes with bit `off` clear keep
 // the first N/2 values and send the second half to their partner, the others
@@ -373,28 +401,33 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) ll_pair_kernel(LL
 #pragma unroll
         for (int i = 0; i < 3; i++)
 #pragma unroll
-            for (int b = 0; b < 2; b++) x[i][b] = T(0, i, 0) * g[0][b] + T(0, i, 1) * g[1][b] + T(0, i, 2) * g[2][b];
+            for (int b = 0; b < 2; b++) x[i][b] = rdot3(T(0, i, 0), g[0][b], T(0, i, 1), g[1][b], T(0, i, 2), g[2][b]);
 #pragma unroll
         for (int i = 0; i < 3; i++)
 #pragma unroll
             for (int j = 0; j < 3; j++) Y[i][j] = C{(R)(i == j), 0};
         if (M >= 2) {
+            // the first eigenstate's phase is 1: its row is not multiplied
             const C d1[3] = {C{1, 0}, D(1, 1), D(1, 2)};
 #pragma unroll
-            for (int i = 0; i < 3; i++)
+            for (int i = 0; i < 3; i++) {
+                Y[i][0] = C{T(1, i, 0), 0};
 #pragma unroll
-                for (int k = 0; k < 3; k++) Y[i][k] = T(1, i, k) * d1[k];
+                for (int k = 1; k < 3; k++) Y[i][k] = T(1, i, k) * d1[k];
+            }
             for (int l = 2; l < M; l++) {
                 const C dl[3] = {C{1, 0}, D(l, 1), D(l, 2)};
                 C U[3][3];
 #pragma unroll
-                for (int k = 0; k < 3; k++)
+                for (int j = 0; j < 3; j++) {
+                    U[0][j] = Y[0][j];
 #pragma unroll
-                    for (int j = 0; j < 3; j++) U[k][j] = dl[k] * Y[k][j];
+                    for (int k = 1; k < 3; k++) U[k][j] = dl[k] * Y[k][j];
+                }
 #pragma unroll
                 for (int i = 0; i < 3; i++)
 #pragma unroll
-                    for (int j = 0; j < 3; j++) Y[i][j] = T(l, i, 0) * U[0][j] + T(l, i, 1) * U[1][j] + T(l, i, 2) * U[2][j];
+                    for (int j = 0; j < 3; j++) Y[i][j] = rdot3(T(l, i, 0), U[0][j], T(l, i, 1), U[1][j], T(l, i, 2), U[2][j]);
             }
         }
         DM[1] = D(M, 1);
@@ -405,17 +438,17 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) ll_pair_kernel(LL
             for (int j = 0; j < 3; j++) {
                 C s{0, 0};
 #pragma unroll
-                for (int k = 0; k < 3; k++) s = s + Y[k][i] * (DM[k] * Y[k][j]);
+                for (int k = 0; k < 3; k++) s = cmac(s, Y[k][i], DM[k] * Y[k][j]);
                 G[i][j] = s;
             }
 #pragma unroll
         for (int k = 0; k < 3; k++)
 #pragma unroll
-            for (int b = 0; b < 2; b++) X[k][b] = G[k][0] * x[0][b] + G[k][1] * x[1][b] + G[k][2] * x[2][b];
+            for (int b = 0; b < 2; b++) X[k][b] = cmac(cmac(G[k][0] * x[0][b], G[k][1], x[1][b]), G[k][2], x[2][b]);
 #pragma unroll
         for (int b = 0; b < 2; b++) {
-            B[0][b] = La[0] * X[0][b] + La[1] * X[1][b] + La[2] * X[2][b];
-            B[1][b] = Lb[0] * X[0][b] + Lb[1] * X[1][b] + Lb[2] * X[2][b];
+            B[0][b] = rdot3(La[0], X[0][b], La[1], X[1][b], La[2], X[2][b]);
+            B[1][b] = cmac(cmac(Lb[0] * X[0][b], Lb[1], X[1][b]), Lb[2], X[2][b]);
         }
     } else {
         // block = Gamma'^dagger D_0 Gamma'
@@ -522,8 +555,8 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) ll_pair_kernel(LL
                 C s{0, 0};
 #pragma unroll
                 for (int j = 0; j < 3; j++) {
-                    s = s + cjmul(Y[k][j], gG[i][j] + gG[j][i]);
-                    sd = sd + cjmul(Y[k][i] * Y[k][j], gG[i][j]);
+                    s = cjmac(s, Y[k][j], gG[i][j] + gG[j][i]);
+                    sd = cjmac(sd, Y[k][i] * Y[k][j], gG[i][j]);
                 }
                 gY[k][i] = cjmul(DM[k], s);
             }
@@ -573,26 +606,31 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) ll_pair_kernel(LL
             for (int k = 0; k < 3; k++)
 #pragma unroll
                 for (int j = 0; j < 3; j++) {
-                    U[k][j] = t[0][k] * Y[0][j] + t[1][k] * Y[1][j] + t[2][k] * Y[2][j];
-                    gU[k][j] = t[0][k] * gY[0][j] + t[1][k] * gY[1][j] + t[2][k] * gY[2][j];
+                    U[k][j] = rdot3(t[0][k], Y[0][j], t[1][k], Y[1][j], t[2][k], Y[2][j]);
+                    gU[k][j] = rdot3(t[0][k], gY[0][j], t[1][k], gY[1][j], t[2][k], gY[2][j]);
                 }
 #pragma unroll
             for (int i = 0; i < 3; i++)
 #pragma unroll
-                for (int k = 0; k < 3; k++)
-                    tT[3 * i + k] = (cjmul(U[k][0], gY[i][0]) + cjmul(U[k][1], gY[i][1]) + cjmul(U[k][2], gY[i][2])).re;
+                for (int k = 0; k < 3; k++) tT[3 * i + k] = cjdot3_re(U[k][0], gY[i][0], U[k][1], gY[i][1], U[k][2], gY[i][2]);
             if (l >= 2) {
+                // row 0: the first eigenstate's phase is 1
 #pragma unroll
-                for (int k = 0; k < 3; k++) {
+                for (int j = 0; j < 3; j++) {
+                    Y[0][j] = U[0][j];
+                    gY[0][j] = gU[0][j];
+                }
+#pragma unroll
+                for (int k = 1; k < 3; k++) {
                     C gd{0, 0};
 #pragma unroll
                     for (int j = 0; j < 3; j++) {
                         const C yp = cjmul(dl[k], U[k][j]);  // Y_{l-1}[k][j]
-                        gd = gd + cjmul(yp, gU[k][j]);
+                        gd = cjmac(gd, yp, gU[k][j]);
                         Y[k][j] = yp;
                         gY[k][j] = cjmul(dl[k], gU[k][j]);
                     }
-                    if (k > 0) tk[k - 1] = -twopi * src.L(l) * cjmul(gd, dl[k]).im;
+                    tk[k - 1] = -twopi * src.L(l) * cjmul(gd, dl[k]).im;
                 }
             } else {
                 // l = 1: Y_1 = T_1 D_1, so U = D_1 and gU holds the adjoint of D_1 on the diagonal
