@@ -72,33 +72,43 @@ template <class T>
 __device__ __forceinline__ Cx<T> cjmul(Cx<T> a, Cx<T> b) {
     return Cx<T>{a.re * b.re + a.im * b.im, a.re * b.im - a.im * b.re};
 }
-// a b + c, fused (one rounding), in the kernel's precision
-__device__ __forceinline__ float fm(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+// Sums of products in the pair kernel.  FP64 (DFMA-bound): chains of fused
+// multiply-adds, the fewest FP64 instructions.  FP32 (bound by latency, not
+// by instruction count): products summed in pairs as the plain expressions
+// compile (fmul / ffma, then adds), whose rounding errors grow more slowly
+// than a chain's where the terms cancel.
 __device__ __forceinline__ double fm(double a, double b, double c) { return __fma_rn(a, b, c); }
-// s + conj(a) b as four fused multiply-adds
-template <class T>
-__device__ __forceinline__ Cx<T> cjmac(Cx<T> s, Cx<T> a, Cx<T> b) {
-    return Cx<T>{fm(a.im, b.im, fm(a.re, b.re, s.re)), fm(-a.im, b.re, fm(a.re, b.im, s.im))};
+// s + conj(a) b
+__device__ __forceinline__ Cx<double> cjmac(Cx<double> s, Cx<double> a, Cx<double> b) {
+    return Cx<double>{fm(a.im, b.im, fm(a.re, b.re, s.re)), fm(-a.im, b.re, fm(a.re, b.im, s.im))};
 }
-// s + a b as four fused multiply-adds
-template <class T>
-__device__ __forceinline__ Cx<T> cmac(Cx<T> s, Cx<T> a, Cx<T> b) {
-    return Cx<T>{fm(-a.im, b.im, fm(a.re, b.re, s.re)), fm(a.im, b.re, fm(a.re, b.im, s.im))};
+__device__ __forceinline__ Cx<float> cjmac(Cx<float> s, Cx<float> a, Cx<float> b) { return s + cjmul(a, b); }
+// s + a b
+__device__ __forceinline__ Cx<double> cmac(Cx<double> s, Cx<double> a, Cx<double> b) {
+    return Cx<double>{fm(-a.im, b.im, fm(a.re, b.re, s.re)), fm(a.im, b.re, fm(a.re, b.im, s.im))};
 }
-// Re(conj(a0) b0 + conj(a1) b1 + conj(a2) b2) as one chain of multiply-adds
-template <class T>
-__device__ __forceinline__ T cjdot3_re(Cx<T> a0, Cx<T> b0, Cx<T> a1, Cx<T> b1, Cx<T> a2, Cx<T> b2) {
-    T s = a0.re * b0.re;
+__device__ __forceinline__ Cx<float> cmac(Cx<float> s, Cx<float> a, Cx<float> b) { return s + a * b; }
+// Re(conj(a0) b0 + conj(a1) b1 + conj(a2) b2)
+__device__ __forceinline__ double cjdot3_re(Cx<double> a0, Cx<double> b0, Cx<double> a1, Cx<double> b1,
+                                            Cx<double> a2, Cx<double> b2) {
+    double s = a0.re * b0.re;
     s = fm(a0.im, b0.im, s);
     s = fm(a1.re, b1.re, s);
     s = fm(a1.im, b1.im, s);
     s = fm(a2.re, b2.re, s);
     return fm(a2.im, b2.im, s);
 }
-// t0 z0 + t1 z1 + t2 z2 for real t as chains of multiply-adds
-template <class T>
-__device__ __forceinline__ Cx<T> rdot3(T t0, Cx<T> z0, T t1, Cx<T> z1, T t2, Cx<T> z2) {
-    return Cx<T>{fm(t2, z2.re, fm(t1, z1.re, t0 * z0.re)), fm(t2, z2.im, fm(t1, z1.im, t0 * z0.im))};
+__device__ __forceinline__ float cjdot3_re(Cx<float> a0, Cx<float> b0, Cx<float> a1, Cx<float> b1, Cx<float> a2,
+                                           Cx<float> b2) {
+    return (cjmul(a0, b0) + cjmul(a1, b1) + cjmul(a2, b2)).re;
+}
+// t0 z0 + t1 z1 + t2 z2 for real t
+__device__ __forceinline__ Cx<double> rdot3(double t0, Cx<double> z0, double t1, Cx<double> z1, double t2,
+                                            Cx<double> z2) {
+    return Cx<double>{fm(t2, z2.re, fm(t1, z1.re, t0 * z0.re)), fm(t2, z2.im, fm(t1, z1.im, t0 * z0.im))};
+}
+__device__ __forceinline__ Cx<float> rdot3(float t0, Cx<float> z0, float t1, Cx<float> z1, float t2, Cx<float> z2) {
+    return t0 * z0 + t1 * z1 + t2 * z2;
 }
 
 // One halving step of a many-value warp sum: lanes with bit `off` clear keep

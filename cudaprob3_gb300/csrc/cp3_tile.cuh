@@ -458,6 +458,10 @@ __device__ __forceinline__ void process_tile(const TileJob& j, int nl, int nl_pa
     Acc r0 = 0, r1 = 0, r2 = 0;
     int run_cb = -1;
     const int my_eb = (RATES && store) ? j.ebin[e] : -1;
+    // a warp whose energies all lie past the grid (the last, partial tile of
+    // a grid whose energy count is not a multiple of TE) has nothing to do
+    // (no barrier follows in this function; callers synchronise after it)
+    if (j.etile * TE + (lane & ~31) >= j.n_en) return;
     for (int cl = threadIdx.y; cl < j.ncl; cl += blockDim.y) {
         const int M = CP3_IX(kSiteTileLayers, s_maxl[cl], nl);
         const int ci = j.c0 + cl;
