@@ -339,8 +339,8 @@ int cp3_loglik_io_bytes(cp3_loglik* L, long long* host_to_device, long long* dev
  * larger problems are rejected with CP3_ERR_LIMIT, and nothing is allocated
  * (no cudaMalloc, cudaFree or allocating library call).  The first call on a
  * device sets that device up: it looks up the array's device address
- * (cudaGetSymbolAddress) and copies the phase tables into it synchronously,
- * so make that first call before any stream capture.  Every call shares the
+ * (cudaGetSymbolAddress) and copies the phase tables into it synchronously
+ * (the only host-synchronous step of the call).  Every call shares the
  * array, which keeps the last call's contents; each call rewrites what it
  * reads before reading it, but calls whose work overlaps on the GPU (other
  * streams or host threads) race on it and must be serialised by the caller.
