@@ -205,7 +205,7 @@ struct LLArgs {
     // float shadows of the tables for the mixed pair kernel (null for FP64)
     float* tabf;     // tile-major [n_en_pad/32][nl][13][32]
     float* pef;      // [18][n_en_pad]
-    float2* lenf;    // [n_cos][nl_pad], hi/lo
+    float2* lenf;    // [nl_pad][n_cos], hi/lo (layer-major: a warp's 32 cosines are adjacent)
     const double2* ptab;  // 257-entry FP64 phase table (cos, sin of 2 pi j / 256)
 };
 
@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(256) ll_prep_kernel(LLArgs a) {
         if (a.lenf) {
             const double L = a.len[(size_t)c * a.nl_pad + l];
             const float h = f32_rn(L);
-            a.lenf[(size_t)c * a.nl_pad + l] = make_float2(h, f32_rn(L - f64_of(h)));
+            a.lenf[(size_t)l * a.n_cos + c] = make_float2(h, f32_rn(L - f64_of(h)));
         }
     }
 }
@@ -346,20 +346,21 @@ template <>
 struct LLSrc<float> {
     const float* f;      // this energy's column of layer 0 in the tile-major shadow
     const float* pef;
-    const float2* len;
-    int e, n_en_pad;
+    const float2* len;   // this cosine's column of the layer-major lengths
+    int e, n_en_pad, n_cos;
     __device__ __forceinline__ LLSrc(const LLArgs& a, int e_, int c)
         : f(a.tabf + (size_t)(e_ / kLLTile) * a.nl * kLLFWords * kLLTile + e_ % kLLTile),
           pef(a.pef),
-          len(a.lenf + (size_t)c * a.nl_pad),
+          len(a.lenf + c),
           e(e_),
-          n_en_pad(a.n_en_pad) {}
+          n_en_pad(a.n_en_pad),
+          n_cos(a.n_cos) {}
     __device__ __forceinline__ float T(int l, int i, int j) const { return f[(l * kLLFWords + 3 * i + j) * kLLTile]; }
     __device__ __forceinline__ Cx<float> D(int l, int k) const {
         const float kh = f[(l * kLLFWords + 7 + 2 * k) * kLLTile], kl = f[(l * kLLFWords + 8 + 2 * k) * kLLTile];
-        return phase_of(make_float2(kh, kl), len[l]);
+        return phase_of(make_float2(kh, kl), len[(size_t)l * n_cos]);
     }
-    __device__ __forceinline__ float L(int l) const { return len[l].x; }
+    __device__ __forceinline__ float L(int l) const { return len[(size_t)l * n_cos].x; }
     __device__ __forceinline__ float pe(int w) const { return pef[(size_t)w * n_en_pad + e]; }
 };
 
