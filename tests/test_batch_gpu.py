@@ -41,6 +41,10 @@ def test_batch_matches_oracle(gpu, precision, tol, anti):
         # the same work as two launches per set gives identical results
         b.calculate_sequential(1 if anti else 0)
         assert np.array_equal(b.results(), flat)
+        # one prep launch per chunk (at most 8) and one propagate launch per
+        # chunk that holds work items
+        n = b.launch_count(1 if anti else 0)
+        assert 2 <= n <= 16
 
 
 def _prem59():

@@ -92,6 +92,16 @@ def test_gradient_is_deterministic_and_moves_with_parameters(problem):
     assert c[0] > a[0]  # the observed point fits its own data better
 
 
+def test_loglik_io_bytes(problem):
+    with problem.make(precision="mixed") as L:
+        up, down = L.io_bytes()
+    rows = len(problem.body.radii)
+    # one row per energy back (its log-likelihood term and 6 + rows gradient
+    # terms, doubles); the parameter block and one rho*Ye per layer up
+    assert down == 8 * len(problem.energies) * (7 + rows)
+    assert 8 * (rows + 1) < up < 4096
+
+
 def test_loglik_errors(gpu):
     from cudaprob3_gb300 import CP3Error
     from cudaprob3_gb300.loglik import LogLikelihood
