@@ -8,8 +8,9 @@
 // layout [9][n_cos_s][n_en_s] at element offset out_offset[s].
 //
 // Device work:
-//   batch_prep_kernel       FP64 eigen data of every (set, energy, layer) and
-//                           segment lengths of every (set, cosine, layer)
+//   batch_prep_kernel       eigen data of every (set, energy, layer) (double-float
+//                           solve for the mixed tables, FP64 for the FP64 ones)
+//                           and segment lengths of every (set, cosine, layer)
 //   batch_propagate_kernel  persistent: each block takes (set, energy tile,
 //                           cosine chunk) items from an atomic counter, largest
 //                           items first, and runs process_tile on them

@@ -12,7 +12,9 @@
 //
 // Launches of one evaluation (captured in a CUDA graph together with the
 // parameter upload and the result download):
-//   ll_prep_kernel    FP64 tables of every (energy, layer) and segment lengths
+//   ll_prep_kernel    eigen tables of every (energy, layer) (FP64, or the
+//                     double-float solve writing the float tables of the mixed
+//                     pair kernel) and segment lengths
 //   ll_pair_kernel    one warp = one energy x 32 cosines; forward chain, LL and
 //                     seeds, then the backward pass that recomputes each layer
 //                     matrix from the tables (no per-layer storage: the chain is
@@ -24,8 +26,9 @@
 //                     eigen-decomposition to the parameters
 // The per-energy rows land in mapped host memory; the host sums them over the
 // energies in a fixed order (deterministic) after the graph completes.
-// Precision: FP64 does every step in double; MIXED runs ll_pair_kernel in
-// FP32 (phases in double-float) with the FP64 tables, sums its float partials
+// Precision: FP64 does every step in double; MIXED solves the layers in
+// double-float arithmetic, runs ll_pair_kernel in FP32 (phases in
+// double-float) on float tables, sums its float partials
 // over the cosine chunks by compensated FP32 sums and does the eigen
 // back-propagation in FP64.
 #include <cuda_runtime.h>
