@@ -118,3 +118,50 @@ def test_parameter_and_body_extremes(gpu, precision, case):
             s = got.reshape(3, 3, c.size, e.size)
             for k in range(3):
                 assert np.abs(s[k, k] - 1.0).max() <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_output_beyond_32_bit_element_indices(gpu, precision):
+    """A 16384 x 16384 grid: its nine planes hold 2.4e9 elements, more than a
+    32-bit index reaches, so every offset of the writeback and of the host
+    copy must be 64-bit.  Pairs spread over the grid up to the far corner of
+    the last plane against the oracle, and over every pair on the device:
+    the rows of |S|^2 (planes in*3 + out, out = 0..2) sum to one.  For the
+    mixed planes, getProbability at the far corner through the handle's own
+    buffer and its host copy."""
+    torch = pytest.importorskip("torch")
+    n = 16384
+    c, e = G.linspace(-1, 0, n), G.logspace(0.1, 1000, n)
+    B = G.PREM_12
+    dt = torch.float32 if precision == "mixed" else torch.float64
+    buf = torch.empty((9, n, n), dtype=dt, device="cuda:0")
+    assert buf.numel() > 2**31
+    with gpu.CudaPropagatorSingle(0, n, n, precision=precision) as p:
+        p.setEnergyList(e)
+        p.setCosineList(c)
+        p.setMNSMatrix(*G.NOMINAL[:4])
+        p.setNeutrinoMasses(*G.NOMINAL[4:])
+        p.setDensity(B.radii, B.rhos, B.ye)
+        p.setProductionHeight(22.0)
+        p.set_result_buffer(buf.data_ptr(), buf.numel() * buf.element_size())
+        p.calculateProbabilities(gpu.Neutrino)
+        torch.cuda.synchronize()
+    idx = np.r_[0:n:2048, n - 1]
+    want = oracle.calculate(c[idx], e[idx], B.radii, B.rho_eff(), G.NOMINAL, 22.0, False)
+    got = buf[:, idx][:, :, idx].double().cpu().numpy()
+    assert np.abs(got - want).max() <= TOL[precision]
+    rows = buf.view(3, 3, n, n).sum(dim=1, dtype=torch.float64)
+    assert float((rows - 1.0).abs().max()) <= (1e-6 if precision == "mixed" else 1e-12)
+    del rows, buf
+    torch.cuda.empty_cache()
+    if precision == "mixed":
+        with gpu.CudaPropagatorSingle(0, n, n, precision=precision) as p:
+            p.setEnergyList(e)
+            p.setCosineList(c)
+            p.setMNSMatrix(*G.NOMINAL[:4])
+            p.setNeutrinoMasses(*G.NOMINAL[4:])
+            p.setDensity(B.radii, B.rhos, B.ye)
+            p.setProductionHeight(22.0)
+            p.calculateProbabilities(gpu.Neutrino)
+            for t in (0, 4, 8):
+                assert abs(p.getProbability(n - 1, n - 1, t) - want[t, -1, -1]) <= TOL[precision]
