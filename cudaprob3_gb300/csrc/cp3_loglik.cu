@@ -210,6 +210,7 @@ struct LLArgs {
     float* pef;      // [18][n_en_pad]
     float2* lenf;    // [nl_pad][n_cos], hi/lo (layer-major: a warp's 32 cosines are adjacent)
     const double2* ptab;  // 257-entry FP64 phase table (cos, sin of 2 pi j / 256)
+    int phase_cache;      // ll_pair_kernel keeps the forward phases in shared memory (ll_pair_cache_bytes)
 };
 
 // ---------------------------------------------------------------- prep ----
@@ -367,6 +368,17 @@ struct LLSrc<float> {
     __device__ __forceinline__ float pe(int w) const { return pef[(size_t)w * n_en_pad + e]; }
 };
 
+// Shared memory of ll_pair_kernel's phase cache: the forward pass's e^{i psi_k}
+// of layers 1 .. nl-1, k = 1, 2, for the block's 128 threads, so that the
+// backward pass reads them instead of evaluating them again.  Zero (no cache:
+// the phases are evaluated twice) where it would cost occupancy: above 56 KB
+// per block for the float kernel (4 blocks per SM) and 110 KB for the double
+// kernel (2 blocks per SM).
+__host__ __device__ inline size_t ll_pair_cache_bytes(bool mixed, int nl) {
+    const size_t b = (size_t)nl * 2 * 128 * (mixed ? 2 * sizeof(float) : 2 * sizeof(double));
+    return b <= (mixed ? 56u : 110u) * 1024 ? b : 0;
+}
+
 template <class R>
 __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) ll_pair_kernel(LLArgs a) {
     using C = Cx<R>;
@@ -396,6 +408,18 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) ll_pair_kernel(LL
     }
     auto T = [&](int l, int i, int j) -> R { return src.T(l, i, j); };
     auto D = [&](int l, int k) -> C { return src.D(l, k); };  // k = 1, 2
+    // the forward pass's phases of layers 1 .. M-1, kept for the backward
+    // pass when the kernel has the shared memory ([layer][k][thread])
+    extern __shared__ __align__(16) unsigned char s_pair_raw[];
+    C* s_ph = (C*)s_pair_raw;
+    const bool cache = a.phase_cache != 0;
+    auto keep = [&](int l, const C d[3]) {
+        if (cache) {
+            s_ph[((size_t)l * 2 + 0) * blockDim.x + threadIdx.x] = d[1];
+            s_ph[((size_t)l * 2 + 1) * blockDim.x + threadIdx.x] = d[2];
+        }
+    };
+    auto Dk = [&](int l, int k) -> C { return cache ? s_ph[((size_t)l * 2 + k - 1) * blockDim.x + threadIdx.x] : D(l, k); };
 
     // ---------------- forward
     C D0[3] = {C{1, 0}, D(0, 1), D(0, 2)};
@@ -423,6 +447,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) ll_pair_kernel(LL
         if (M >= 2) {
             // the first eigenstate's phase is 1: its row is not multiplied
             const C d1[3] = {C{1, 0}, D(1, 1), D(1, 2)};
+            keep(1, d1);
 #pragma unroll
             for (int i = 0; i < 3; i++) {
                 Y[i][0] = C{T(1, i, 0), 0};
@@ -431,6 +456,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) ll_pair_kernel(LL
             }
             for (int l = 2; l < M; l++) {
                 const C dl[3] = {C{1, 0}, D(l, 1), D(l, 2)};
+                keep(l, dl);
                 C U[3][3];
 #pragma unroll
                 for (int j = 0; j < 3; j++) {
@@ -609,7 +635,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) ll_pair_kernel(LL
             for (int k = 1; k < 3; k++) tk[k - 1] = -twopi * src.L(l) * cjmul(gDM[k], DM[k]).im;
         } else if (l < M) {
             // Y_l = T_l U, U = D_l Y_{l-1}; un-multiply: U = T_l^T Y_l, Y_{l-1} = conj(D_l) U
-            const C dl[3] = {C{1, 0}, D(l, 1), D(l, 2)};
+            const C dl[3] = {C{1, 0}, Dk(l, 1), Dk(l, 2)};
             R t[3][3];
 #pragma unroll
             for (int i = 0; i < 3; i++)
@@ -1109,6 +1135,7 @@ cp3::LLArgs ll_args(cp3_loglik* L, int type) {
     a.pef = L->mixed ? L->d_pef : nullptr;
     a.lenf = L->mixed ? L->d_lenf : nullptr;
     a.ptab = (const double2*)L->d_ptab;
+    a.phase_cache = cp3::ll_pair_cache_bytes(L->mixed, L->nl) > 0;
     a.part_l_f = L->mixed ? L->d_plf : nullptr;
     a.part_e_f = L->mixed ? L->d_peef : nullptr;
     a.flux_e_f = L->d_fef;
@@ -1170,6 +1197,12 @@ int ll_setup(cp3_loglik* L, int type) {
         ((e = cudaMalloc(&L->d_tabf, (size_t)L->n_en_pad * L->nl * cp3::kLLFWords * 4)) ||
          (e = cudaMalloc(&L->d_pef, (size_t)18 * L->n_en_pad * 4)) || (e = cudaMalloc(&L->d_lenf, len * 8))))
         return lcuda(e, "cudaMalloc(loglik)");
+    // the pair kernel's phase cache may take more than the default 48 KB of
+    // dynamic shared memory (opted in per device, before the capture)
+    const size_t pair_smem = cp3::ll_pair_cache_bytes(L->mixed, L->nl);
+    if (pair_smem > 48 * 1024 &&
+        (e = cp3::opt_in_max_smem(L->mixed ? (const void*)cp3::ll_pair_kernel<float> : (const void*)cp3::ll_pair_kernel<double>)))
+        return lcuda(e, "cudaFuncSetAttribute(ll_pair_kernel)");
     // capture
     cudaStream_t cs;
     if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking))) return lcuda(e, "cudaStreamCreate");
@@ -1196,9 +1229,9 @@ int ll_setup(cp3_loglik* L, int type) {
     if (!e) {
         dim3 grid((L->n_en + 3) / 4, L->n_cchunk);
         if (L->mixed)
-            cp3::ll_pair_kernel<float><<<grid, 128, 0, cs>>>(a);
+            cp3::ll_pair_kernel<float><<<grid, 128, pair_smem, cs>>>(a);
         else
-            cp3::ll_pair_kernel<double><<<grid, 128, 0, cs>>>(a);
+            cp3::ll_pair_kernel<double><<<grid, 128, pair_smem, cs>>>(a);
         e = cudaGetLastError();
     }
     stamp(2);
