@@ -78,11 +78,12 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a) {
 }
 
 // ------------------------------------------------------------ propagate ----
-// Mixed planes and rates: 4 blocks of 256 threads per SM (64 registers, no
-// spill: the atmosphere segment is formed after the layer chain); the
-// height-average mode and FP64 keep 3 (more live values).
+// Mixed: 4 blocks of 256 threads per SM (64 registers; planes and height
+// averages without spill: the atmosphere segment is formed after the layer
+// chain; the height-average mode ran 1.2 % faster at 4 blocks than at 3);
+// FP64: 3 blocks of 128 threads.
 template <bool MIXED, int TE, int MODE>
-__global__ void __launch_bounds__(MIXED ? 256 : 128, (MIXED && MODE != kModeHeights) ? 4 : 3)
+__global__ void __launch_bounds__(MIXED ? 256 : 128, MIXED ? 4 : 3)
     propagate_kernel(PropArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const TileSmem L = tile_smem(MIXED, TE, a.nl, a.nl_pad, a.cchunk);
