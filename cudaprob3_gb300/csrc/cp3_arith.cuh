@@ -337,8 +337,9 @@ struct F64 {
 // Taylor series of sin to x^5 and of cos - 1 to x^6 (truncation below
 // 1e-17), written in d with 2 pi folded into the coefficients, rotated onto
 // entry (j + 128) mod 256 of the 257-entry table of cos, sin of
-// 2 pi (k - 128) / 256.  Fifteen FP64 instructions in all, the table index on
-// the integer pipe.
+// 2 pi (k - 128) / 256.  Fifteen FP64 instructions in all for a given t,
+// fourteen for a product kappa * L (reduce_product_f64 below), the table
+// index on the integer pipe.
 __device__ __forceinline__ void reduce_turns_f64(double t, int& j, double& d) {
     const double magic = 6755399441055744.0;  // 1.5 * 2^52
     const double y = fma(t, 256.0, magic);
@@ -369,9 +370,25 @@ __device__ __forceinline__ void sincos_turns_f64(double t, const double2* __rest
     sincos_reduced_f64(j, d, tab, c, s);
 }
 
+// The reduction of a product t = kappa * L without rounding t first: adding
+// 1.5 * 2^44 to the fused product rounds it to a multiple of 1/256 (the sum's
+// last place), whose count j sits in the sum's low word as above, and
+// d = kappa * L - j / 256 comes from a second fused multiply-add with the
+// exact -j / 256 = 1.5 * 2^44 - y: three FP64 instructions instead of four,
+// and d carries one rounding of itself instead of the rounding of t.
+__device__ __forceinline__ void reduce_product_f64(double kappa, double L, int& j, double& d) {
+    const double magic = 26388279066624.0;  // 1.5 * 2^44
+    const double y = fma(kappa, L, magic);
+    j = __double2loint(y);
+    d = fma(kappa, L, magic - y);
+}
+
 // FP64 cos/sin of 2*pi*t, t = kappa * L turns.
 __device__ __forceinline__ void phase_f64(double kappa, double L, const double2* tab, double& c, double& s) {
-    sincos_turns_f64(kappa * L, tab, c, s);
+    int j;
+    double d;
+    reduce_product_f64(kappa, L, j, d);
+    sincos_reduced_f64(j, d, tab, c, s);
 }
 
 }  // namespace cp3

@@ -274,8 +274,8 @@ struct F64Src {
         const double* k = tab + (l * kFp64Words + 9) * TE;
         int j1, j2;
         double d1, d2;
-        reduce_turns_f64(k[0] * L, j1, d1);
-        reduce_turns_f64(k[TE] * L, j2, d2);
+        reduce_product_f64(k[0], L, j1, d1);
+        reduce_product_f64(k[TE], L, j2, d2);
         sincos_reduced_f64(j1, d1, ptab, c1, s1);
         sincos_reduced_f64(j2, d2, ptab, c2, s2);
         n1 = -s1;
