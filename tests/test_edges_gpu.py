@@ -11,7 +11,9 @@
     layer count and the chord lengths switch (propagator.hpp:149-158,
     301-307; physics.hpp:555-580);
   * no mixing (all angles zero: the eigenvectors are the axes, P = identity),
-    maximal mixing, and a body of vacuum rows (zero density).
+    maximal mixing, and a body of vacuum rows (zero density);
+  * random bodies and parameters;
+  * a grid whose planes pass 2^31 elements.
 Tolerances: FP64 1e-11 (2e-10 at the highest energies), mixed 1e-6."""
 import numpy as np
 import pytest
@@ -165,3 +167,31 @@ def test_output_beyond_32_bit_element_indices(gpu, precision):
             p.calculateProbabilities(gpu.Neutrino)
             for t in (0, 4, 8):
                 assert abs(p.getProbability(n - 1, n - 1, t) - want[t, -1, -1]) <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_random_bodies(gpu, precision):
+    """Random bodies (1-20 rows, outermost radius 6371 km, the rest strictly
+    decreasing at random spacings, with or without a radius-0 row; densities
+    0-15 g/cm^3, electron fractions 0.40-0.60, rows given outside-in or
+    inside-out), random oscillation parameters of either ordering, both
+    neutrino types, cosines over [-1, 1]: both kernels against the oracle."""
+    rng = np.random.default_rng(11)
+    c, e = G.linspace(-1, 1, 23), G.logspace(0.2, 200.0, 29)
+    for trial in range(8):
+        n = int(rng.integers(1, 21))
+        inner = np.sort(rng.uniform(0.0, R_EARTH, size=n - 1))[::-1]
+        radii = np.concatenate([[R_EARTH], inner])
+        if n > 1 and rng.random() < 0.5:
+            radii[-1] = 0.0
+        if len(np.unique(radii)) != n:
+            continue
+        rhos = rng.uniform(0.0, 15.0, size=n)
+        ye = rng.uniform(0.40, 0.60, size=n)
+        if rng.random() < 0.5:  # inside-out order
+            radii, rhos, ye = radii[::-1].copy(), rhos[::-1].copy(), ye[::-1].copy()
+        params = tuple(G.draw_parameter_sets(1, seed=100 + trial)[0])
+        anti = bool(trial & 1)
+        got = run(gpu, precision, c, e, radii, rhos, ye, params, anti)
+        want = oracle.calculate(c, e, radii, rhos * ye / 0.5, params, 22.0, anti)
+        assert np.abs(got - want).max() <= TOL[precision], (trial, n, precision)
