@@ -63,6 +63,14 @@ class LogLikelihood:
         y = None if ye is None else np.ascontiguousarray(ye, dtype=np.float64)
         check(self._lib.cp3_loglik_set_body(self._h, _dp(r), None if y is None else _dp(y), int(r.size)))
         self.n_rows = int(r.size)
+        # argument buffers of evaluate, with their ctypes pointers made once:
+        # building the pointers and arrays on every call costs about 7 us on
+        # the GPU machine's host, more than a tenth of a mixed evaluation
+        self._p = np.zeros(6)
+        self._r = np.zeros(self.n_rows)
+        self._g = np.zeros(6 + self.n_rows)
+        self._ll = ctypes.c_double()
+        self._args = (_dp(self._p), _dp(self._r), ctypes.byref(self._ll), _dp(self._g))
 
     def set_production_height(self, km):
         check(self._lib.cp3_loglik_set_production_height(self._h, float(km)))
@@ -77,12 +85,19 @@ class LogLikelihood:
         check(self._lib.cp3_loglik_set_observed(self._h, _dp(n)))
 
     def evaluate(self, params, rhos, ntype=0):
-        p = np.ascontiguousarray(params, dtype=np.float64)
-        r = np.ascontiguousarray(rhos, dtype=np.float64)
-        ll = ctypes.c_double()
-        grad = np.empty(6 + self.n_rows, dtype=np.float64)
-        check(self._lib.cp3_loglik_evaluate(self._h, int(ntype), _dp(p), _dp(r), ctypes.byref(ll), _dp(grad)))
-        return ll.value, grad
+        """(LL, gradient) at the 6 oscillation parameters and the row
+        densities (one per row of the body); the gradient is a new array."""
+        if not self.n_rows:  # no body yet: the C call reports what is missing
+            p = np.ascontiguousarray(params, dtype=np.float64)
+            r = np.ascontiguousarray(rhos, dtype=np.float64)
+            ll = ctypes.c_double()
+            grad = np.empty(6, dtype=np.float64)
+            check(self._lib.cp3_loglik_evaluate(self._h, int(ntype), _dp(p), _dp(r), ctypes.byref(ll), _dp(grad)))
+            return ll.value, grad
+        self._p[:] = params  # raises unless there are 6 parameters and n_rows densities
+        self._r[:] = rhos
+        check(self._lib.cp3_loglik_evaluate(self._h, int(ntype), *self._args))
+        return self._ll.value, self._g.copy()
 
     def set_kernel_timing(self, enable):
         """CUDA events around the evaluation's kernels (the graph is captured
